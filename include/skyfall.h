@@ -1,0 +1,241 @@
+/*
+ * skyfall.h -- C-ABI of the GB300 Gaussian-splat render-and-train library.
+ *
+ * The library replaces the hot path of Skyfall-Viewer's GaussianRenderer
+ * (src/renderers/gaussian-renderer.ts): projection, tile-key emission, the
+ * intersection radix sort, tile ranges, the tiled forward rasterizer, the
+ * loss, the tiled backward, the geometry backward, Adam, and prune/densify
+ * compaction.  Every entry point returns an int status (SKY_OK == 0, negative
+ * on error); sky_last_error() returns a thread-local message for the last
+ * failing call on the calling thread.
+ *
+ * Ownership: the library owns all device memory of a context.  Host arrays
+ * passed in are copied before the call returns and are never retained.
+ * Threading: one context is used by one thread at a time; distinct contexts
+ * are independent.  All plain types, no C++ or torch types cross the ABI.
+ */
+#ifndef SKYFALL_H
+#define SKYFALL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define SKY_OK 0
+#define SKY_ERR_ARG (-1)      /* invalid argument or size                  */
+#define SKY_ERR_OOM (-2)      /* device or host allocation failed          */
+#define SKY_ERR_CUDA (-3)     /* CUDA runtime error                        */
+#define SKY_ERR_TIMEOUT (-4)  /* a bounded device wait gave up             */
+#define SKY_ERR_CAPACITY (-5) /* intersection capacity exceeded (retried)  */
+#define SKY_ERR_STATE (-6)    /* call out of order (no points, no cameras) */
+#define SKY_ERR_INJECTED (-7) /* host-side fault injection (SKY_FAULT)     */
+
+/* ---- parameter layout --------------------------------------------------
+ * Per-Gaussian trainable parameters are 59 f32 planes (structure of arrays),
+ * plane p of Gaussian i at params[p * plane_stride + i].  The planes mirror
+ * the reference's five f32 training buffers (gaussian-renderer.ts:216-221):
+ *   0..2   position x, y, z                  (train_position)
+ *   3..5   log sigma x, y, z                 (train_scale)
+ *   6..9   quaternion x, y, z, w             (train_rotation)
+ *   10     opacity logit                     (train_opacity)
+ *   11..58 SH coefficient k, channel c at 11 + 3k + c (train_sh)
+ */
+#define SKY_PLANE_POS 0
+#define SKY_PLANE_LOGSCALE 3
+#define SKY_PLANE_ROT 6
+#define SKY_PLANE_OPACITY 10
+#define SKY_PLANE_SH 11
+#define SKY_NUM_PLANES 59
+
+/* ---- backward modes ------------------------------------------------------ */
+/* Exact adjoint of the forward (default): every composited splat, the
+ * colour clamp and the view-direction term of the SH colour are
+ * differentiated; per-(tile, intersection) partial sums are reduced in a
+ * fixed order, so gradients are bit-stable from run to run.               */
+#define SKY_BWD_EXACT 0
+/* Reference semantics of backward-tiles-local.wgsl:185-382: splats with
+ * alpha > 0.98 are skipped, each per-pixel value is truncated to i32 fixed
+ * point (x65536) and summed per (tile, intersection) for all 54 values,
+ * then summed per Gaussian exactly in i64.  Used for bit-exact parity.    */
+#define SKY_BWD_REFERENCE 1
+
+/* ---- camera ---------------------------------------------------------------
+ * Mirrors TrainingCameraData / CameraUniforms (src/camera/training-camera.ts:4-15,
+ * src/shaders/common.wgsl:21-28): column-major view (world->camera) and
+ * projection matrices, focal lengths in pixels, and the training image size.
+ */
+typedef struct SkyCamera {
+  float view[16];
+  float proj[16];
+  float focal[2];
+  uint32_t width;
+  uint32_t height;
+} SkyCamera;
+
+/* ---- configuration ---------------------------------------------------------
+ * Defaults (sky_config_default) follow the reference: projection params
+ * (gaussian-renderer.ts:474-488), background (:490-504), learning rates and
+ * schedules (:82-98), Adam constants (:2422-2424), SH schedule (:3625-3636). */
+typedef struct SkyConfig {
+  uint32_t struct_size;        /* sizeof(SkyConfig)                          */
+  uint32_t tile_size;          /* 8, 16 or 32 (reference: 16)                */
+  uint32_t sh_degree;          /* SH degree of the scene, 0..3               */
+  uint32_t sh_degree_interval; /* active degree = min(sh_degree, it/interval) */
+  float near_plane;            /* 0.2                                        */
+  float far_plane;             /* 1e4                                        */
+  float radius_clip;           /* 512                                        */
+  float eps2d;                 /* 0.3                                        */
+  float background[3];         /* 0, 0, 0                                    */
+  float w_l2, w_l1, w_ssim;    /* loss weights                               */
+  float lr_means;              /* 1.6e-4, log-lerp to lr_means_final         */
+  float lr_means_final;        /* 1.6e-6                                     */
+  float lr_means_delay_mult;   /* 0.01                                       */
+  uint32_t lr_means_max_steps; /* 30000                                      */
+  float lr_sh, lr_opacity, lr_scale, lr_rotation;
+  float beta1, beta2, adam_eps;
+  uint32_t sh_update_interval; /* SH planes updated when it % interval == 0  */
+  uint32_t round_params_f16;   /* 1: projection reads f16-rounded params, as
+                                  the reference's packed storage does       */
+  uint32_t backward_mode;      /* SKY_BWD_EXACT or SKY_BWD_REFERENCE         */
+  uint32_t use_graph;          /* capture sky_step as one CUDA graph         */
+  uint32_t max_views_per_step; /* batch size bound (buffers sized for it)    */
+  uint64_t seed;               /* camera choice and densify randomness       */
+} SkyConfig;
+
+typedef struct SkyStepStats {
+  uint64_t iteration;         /* training iteration after this step         */
+  uint64_t num_intersections; /* sum over the step's views                  */
+  double loss;                /* sum over pixels/channels of
+                                 0.5 w_l2 r^2 + w_l1 |r| (no SSIM term)      */
+  uint32_t num_gaussians;
+  uint32_t num_views;
+  uint32_t sh_degree;         /* active SH degree used by this step         */
+  uint32_t sh_updated;        /* 1 if the SH planes took an Adam step       */
+} SkyStepStats;
+
+typedef struct SkyStatus {
+  uint64_t iteration;
+  uint64_t adam_steps;
+  uint64_t last_intersections;
+  uint64_t device_bytes;      /* device memory held by the context          */
+  uint32_t num_gaussians;
+  uint32_t capacity;
+  uint32_t num_cameras;
+  uint32_t error_flags;       /* sticky device error word (0 = none)        */
+} SkyStatus;
+
+/* Prune rule of applyMultiViewPrune (gaussian-renderer.ts:2840-2886) with
+ * the random budget replaced by a seeded one: prunable if
+ * sigmoid(logit) < min_opacity or max(exp(log sigma)) > max_scale.  The
+ * removal set is capped at max_remove_ratio * N when that is > 0.        */
+typedef struct SkyPruneParams {
+  float min_opacity;       /* 0.005                      */
+  float max_scale;         /* scene_extent * 0.1         */
+  float max_remove_ratio;  /* 0 = no cap                 */
+  uint32_t reserved;
+} SkyPruneParams;
+
+/* Densify rule of performDensification (gaussian-renderer.ts:3248-3318). */
+typedef struct SkyDensifyParams {
+  float grad_threshold;      /* 0.003 (scaled by width / 2)     */
+  float grad_abs_threshold;  /* 0.015 (scaled by width / 2)     */
+  float size_threshold;      /* dense_size_ratio * scene_extent */
+  float min_visibility;      /* 25                              */
+  float importance_threshold;/* candidates need importance > it */
+  float max_new_ratio;       /* 0.1                             */
+  float pixel_width;         /* training width for the scaling  */
+  uint32_t reserved;
+} SkyDensifyParams;
+
+/* ---- buffers readable with sky_read_buffer (introspection) -------------- */
+#define SKY_BUF_RECORDS 1      /* per (view, Gaussian) projection record, 12 f32 */
+#define SKY_BUF_COUNTS 2       /* per (view, Gaussian) tile count, u32            */
+#define SKY_BUF_CUMSUM 3       /* inclusive scan of the counts, u32               */
+#define SKY_BUF_KEYS_EMIT 4    /* keys in emission order, u32                     */
+#define SKY_BUF_KEYS_SORTED 5  /* keys after the sort, u32                        */
+#define SKY_BUF_VALS_SORTED 6  /* emission index after the sort, u32              */
+#define SKY_BUF_FLATTEN 7      /* record index per sorted intersection, u32       */
+#define SKY_BUF_TILE_OFFSETS 8 /* tile range starts, total tiles + 1, u32         */
+#define SKY_BUF_COLOR 9        /* rendered rgba f32 per pixel                     */
+#define SKY_BUF_ALPHA 10       /* accumulated alpha f32 per pixel                 */
+#define SKY_BUF_LAST_IDS 11    /* last visited intersection per pixel, u32        */
+#define SKY_BUF_RESIDUAL 12    /* dL/dcolor rgba f32 per pixel                    */
+#define SKY_BUF_PARTIALS 13    /* per intersection (emission order) 12 f32        */
+#define SKY_BUF_TILE_GRADS 14  /* reference mode: 54 i32 per sorted intersection  */
+#define SKY_BUF_GRADS 15       /* 59 gradient planes of the last backward         */
+#define SKY_BUF_GROUPS 16      /* per sort group: begin, end intersection, u32    */
+#define SKY_BUF_STEP_SCALARS 17 /* f32: lr pos, scale, rot, opacity, sh, beta1,
+                                   beta2, eps, bias-correction 1/bc1, 1/sqrt(bc2),
+                                   SH degree, SH-update flag                     */
+
+/* ---- lifecycle ------------------------------------------------------------ */
+void sky_config_default(SkyConfig* cfg);
+int sky_create(const SkyConfig* cfg, void** ctx_out);
+int sky_destroy(void* ctx);
+int sky_set_config(void* ctx, const SkyConfig* cfg); /* mutable fields only   */
+const char* sky_last_error(void);
+int sky_version(void);
+
+/* Builds a training camera exactly as get_pinhole_projection_matrix
+ * (src/camera/training-camera.ts:29-52) does: f64 arithmetic, f32 storage. */
+int sky_camera_pinhole(const float view[16], double fx, double fy, double cx,
+                       double cy, uint32_t width, uint32_t height, SkyCamera* out);
+
+/* ---- scene ------------------------------------------------------------------
+ * sky_load_points replaces reloadPointCloud + training_init_params
+ * (gaussian-renderer.ts:2092-2126, training-params.wgsl:35-79);
+ * sky_load_packed takes the reference's packed f16 buffers (Gaussian = 6 u32
+ * words, SH = 24 u32 words, common.wgsl:39-43).                              */
+int sky_load_points(void* ctx, const float* params, uint32_t n, uint64_t plane_stride);
+int sky_load_packed(void* ctx, const uint32_t* gaussians, const uint32_t* sh, uint32_t n);
+int sky_set_cameras(void* ctx, const SkyCamera* cams, uint32_t n);  /* setTrainingCameras :4084 */
+int sky_set_target(void* ctx, uint32_t camera, const float* rgb, uint32_t width,
+                   uint32_t height);                                /* setTrainingImages :4098 */
+
+/* ---- hot path --------------------------------------------------------------
+ * sky_render: forward only for n cameras; rgba (4 f32) and alpha (1 f32) per
+ * pixel, images concatenated in camera order (either pointer may be NULL).
+ * sky_forward + sky_backward: the forward/backward op pair; sky_forward also
+ * evaluates the loss against the cameras' targets, sky_backward returns the
+ * 59 gradient planes (summed over the forward's views) without an Adam step.
+ * sky_step: one training step over n cameras (trainStep :3638-3660, batched);
+ * sky_train: the reference train(n) loop (:3744-3854) with a seeded camera
+ * choice, one camera per step.                                               */
+int sky_render(void* ctx, const uint32_t* cameras, uint32_t n, float* rgba, float* alpha);
+int sky_forward(void* ctx, const uint32_t* cameras, uint32_t n, double* loss);
+int sky_backward(void* ctx, float* grads, uint64_t plane_stride);
+int sky_step(void* ctx, const uint32_t* cameras, uint32_t n, SkyStepStats* stats);
+int sky_train(void* ctx, uint32_t iterations, uint32_t views_per_step, SkyStepStats* last);
+
+/* ---- prune / densify / opacity reset ------------------------------------ */
+int sky_prune(void* ctx, const SkyPruneParams* p, const uint8_t* mask, uint32_t* removed);
+int sky_densify_stats(void* ctx, float* grad_accum, float* importance); /* 4 f32 each per G */
+int sky_densify(void* ctx, const SkyDensifyParams* p, uint32_t* cloned, uint32_t* split);
+int sky_reset_opacity(void* ctx, float max_opacity);                   /* resetOpacity :3867 */
+
+/* ---- readback ------------------------------------------------------------- */
+int sky_get_params(void* ctx, float* params, uint64_t plane_stride);
+int sky_get_moments(void* ctx, float* m1, float* m2, uint64_t plane_stride);
+int sky_get_count(void* ctx, uint32_t* n);
+int sky_get_status(void* ctx, SkyStatus* st);
+int sky_read_buffer(void* ctx, int which, void* dst, uint64_t bytes, uint64_t* size_out);
+int sky_sync(void* ctx);
+
+/* ---- device-pointer operators --------------------------------------------
+ * Stable LSD radix sort of (u32 key, u32 value) pairs on the low key_bits
+ * bits, replacing get_sorter(...).sort (src/sort/sort.ts:260-370,
+ * radix_sort.wgsl:55-519).  All pointers are device pointers; stream is a
+ * cudaStream_t (NULL = legacy default stream).  Input and output arrays must
+ * not overlap.  Scratch is allocated and cached by the library per device.  */
+int sky_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                   uint32_t* vals_out, uint32_t n, uint32_t key_bits, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SKYFALL_H */

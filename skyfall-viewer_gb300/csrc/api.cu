@@ -1,0 +1,988 @@
+// Host runtime and C-ABI of the skyfall library (include/skyfall.h).
+//
+// A context owns every device buffer of one scene: the 59 f32 parameter
+// planes with their Adam moments, the cameras' target images, and the step
+// buffers (projection records, intersection keys, tile ranges, images,
+// per-intersection partial gradients).  sky_step runs, on one CUDA stream:
+//   preprocess -> scan -> emit keys -> onesweep sort (per group of views) ->
+//   tile ranges -> forward (+loss) -> backward -> geometry adjoint + Adam
+// and, when the context was created with use_graph, replays that sequence as
+// one captured CUDA graph.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "kernels.cuh"
+#include "skyfall.h"
+
+using namespace sky;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+#define CK(x)                                                                        \
+  do {                                                                               \
+    cudaError_t e_ = (x);                                                            \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(e_ == cudaErrorMemoryAllocation ? SKY_ERR_OOM : SKY_ERR_CUDA,       \
+                  "%s failed: %s", #x, cudaGetErrorString(e_));                      \
+  } while (0)
+
+#define TRY(x)                 \
+  do {                         \
+    int r_ = (x);              \
+    if (r_ != SKY_OK) return r_; \
+  } while (0)
+
+// Host-side fault injection for tests of the error paths: SKY_FAULT=alloc:N
+// makes the N-th device allocation (1-based, process wide) fail with
+// SKY_ERR_INJECTED; SKY_FAULT=launch:N makes the N-th step fail before it
+// launches anything.
+struct FaultPlan {
+  long alloc_at = -1, launch_at = -1;
+  long allocs = 0, launches = 0;
+  FaultPlan() {
+    const char* f = getenv("SKY_FAULT");
+    if (!f) return;
+    if (!strncmp(f, "alloc:", 6)) alloc_at = atol(f + 6);
+    if (!strncmp(f, "launch:", 7)) launch_at = atol(f + 7);
+  }
+};
+std::mutex g_fault_mu;
+FaultPlan& faults() {
+  static FaultPlan p;
+  return p;
+}
+bool inject_alloc() {
+  std::lock_guard<std::mutex> l(g_fault_mu);
+  FaultPlan& p = faults();
+  return p.alloc_at > 0 && ++p.allocs == p.alloc_at;
+}
+bool inject_launch() {
+  std::lock_guard<std::mutex> l(g_fault_mu);
+  FaultPlan& p = faults();
+  return p.launch_at > 0 && ++p.launches == p.launch_at;
+}
+
+uint64_t splitmix64(uint64_t& s) {
+  uint64_t z = (s += 0x9E3779B97F4A7C15ull);
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+// Decimal literal the reference's JavaScript uses for an f32 hyperparameter
+// (0.9f -> 0.9): round the f32 value to 7 significant digits in double.
+double js_literal(float f) {
+  if (f == 0.0f) return 0.0;
+  char buf[64];
+  snprintf(buf, sizeof(buf), "%.7g", (double)f);
+  return strtod(buf, nullptr);
+}
+
+enum Mode { kRender = 0, kForward = 1, kBackward = 2, kTrain = 3 };
+
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct Context {
+  SkyConfig cfg{};
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint32_t n = 0, stride = 0;
+  Buf params, m1, m2, grads, tmp_planes;
+  Buf records, counts, rects, cumsum, block_sums;
+  Buf keys, keys_sorted, vals_sorted, rec_of, flatten, partials, tile_grads, gsum54;
+  Buf offsets, loss_partials, color, alpha, tfinal, last, residual, targets, sort_mem;
+  Buf flags, flag_scan, d_sp, d_st;
+  SortScratch sort{};
+  uint32_t icap = 0;
+  std::vector<SkyCamera> cams;
+  std::vector<uint64_t> tgt_base;
+  std::vector<uint8_t> tgt_set;
+  uint64_t targets_px = 0;
+  StepParams* h_sp = nullptr;
+  DevStatus* h_st = nullptr;
+  uint64_t iteration = 0, adam_steps = 0, last_isect = 0;
+  double last_loss = 0.0;
+  uint64_t rng = 0;
+  size_t device_bytes = 0;
+  // shape of the last step (for readback and sky_backward)
+  std::vector<uint32_t> last_views;
+  uint32_t last_items = 0, last_tiles = 0, last_pixels = 0, last_groups = 0;
+  bool fwd_ready = false;
+  uint32_t error_flags = 0;
+};
+
+int dev_alloc(Context* c, Buf& b, size_t bytes, bool keep = false) {
+  if (bytes <= b.bytes && b.p) return SKY_OK;
+  if (inject_alloc()) return fail(SKY_ERR_INJECTED, "injected allocation failure");
+  size_t want = bytes + bytes / 4 + 256;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(SKY_ERR_OOM, "cudaMalloc(%zu) failed: %s", want, cudaGetErrorString(e));
+  }
+  if (keep && b.p && b.bytes) {
+    CK(cudaMemcpyAsync(p, b.p, b.bytes, cudaMemcpyDeviceToDevice, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  if (b.p) {
+    cudaFree(b.p);
+    c->device_bytes -= b.bytes;
+  }
+  b.p = p;
+  b.bytes = want;
+  c->device_bytes += want;
+  return SKY_OK;
+}
+
+void dev_free(Context* c, Buf& b) {
+  if (b.p) cudaFree(b.p);
+  c->device_bytes -= b.bytes;
+  b.p = nullptr;
+  b.bytes = 0;
+}
+
+DevBuffers make_buffers(Context* c) {
+  DevBuffers b{};
+  b.params = (float*)c->params.p;
+  b.m1 = (float*)c->m1.p;
+  b.m2 = (float*)c->m2.p;
+  b.grads = (float*)c->grads.p;
+  b.records = (float4*)c->records.p;
+  b.counts = (uint32_t*)c->counts.p;
+  b.rects = (uint2*)c->rects.p;
+  b.cumsum = (uint32_t*)c->cumsum.p;
+  b.block_sums = (uint32_t*)c->block_sums.p;
+  b.keys = (uint32_t*)c->keys.p;
+  b.keys_sorted = (uint32_t*)c->keys_sorted.p;
+  b.vals_sorted = (uint32_t*)c->vals_sorted.p;
+  b.rec_of = (uint32_t*)c->rec_of.p;
+  b.flatten = (uint32_t*)c->flatten.p;
+  b.partials = (float4*)c->partials.p;
+  b.tile_grads = (int32_t*)c->tile_grads.p;
+  b.gsum54 = (long long*)c->gsum54.p;
+  b.offsets = (uint32_t*)c->offsets.p;
+  b.loss_partials = (double*)c->loss_partials.p;
+  b.color = (float4*)c->color.p;
+  b.alpha = (float*)c->alpha.p;
+  b.tfinal = (float*)c->tfinal.p;
+  b.last = (uint32_t*)c->last.p;
+  b.residual = (float4*)c->residual.p;
+  b.targets = (const float4*)c->targets.p;
+  b.sp = (const StepParams*)c->d_sp.p;
+  b.status = (DevStatus*)c->d_st.p;
+  return b;
+}
+
+uint32_t ceil_log2(uint32_t x) {
+  uint32_t b = 0;
+  while ((1ull << b) < (uint64_t)x) ++b;
+  return b;
+}
+
+int ensure_isect(Context* c, uint32_t need) {
+  if (need <= c->icap && c->keys.p) return SKY_OK;
+  uint64_t cap = (uint64_t)need + need / 2 + 4096;
+  if (cap > (1u << 30)) cap = 1u << 30;
+  if (need > cap) return fail(SKY_ERR_CAPACITY, "%u intersections exceed the 2^30 limit", need);
+  const bool ref = c->cfg.backward_mode == SKY_BWD_REFERENCE;
+  TRY(dev_alloc(c, c->keys, cap * 4));
+  TRY(dev_alloc(c, c->keys_sorted, cap * 4));
+  TRY(dev_alloc(c, c->vals_sorted, cap * 4));
+  TRY(dev_alloc(c, c->rec_of, cap * 4));
+  TRY(dev_alloc(c, c->flatten, cap * 4));
+  TRY(dev_alloc(c, c->partials, cap * kPartialF4 * 16));
+  if (ref) TRY(dev_alloc(c, c->tile_grads, cap * 54 * 4));
+  TRY(dev_alloc(c, c->sort_mem, sort_scratch_bytes((uint32_t)cap)));
+  c->sort = sort_scratch_carve(c->sort_mem.p, (uint32_t)cap);
+  c->icap = (uint32_t)cap;
+  return SKY_OK;
+}
+
+double position_lr(const SkyConfig& cfg, uint64_t iteration) {
+  // computePositionLearningRate (gaussian-renderer.ts:284-298)
+  const double lr0 = js_literal(cfg.lr_means), lr1 = js_literal(cfg.lr_means_final);
+  if (lr0 <= 0 || lr1 <= 0) return lr0;
+  const double step = (double)iteration;
+  const double max_steps = std::max(1.0, (double)cfg.lr_means_max_steps);
+  const double t = std::min(1.0, step / max_steps);
+  const double log_lerp = std::exp(std::log(lr0) * (1 - t) + std::log(lr1) * t);
+  double delay = 1.0;
+  const double dm = js_literal(cfg.lr_means_delay_mult);
+  if (dm < 0.999) {
+    const double phase = std::min(1.0, step / std::max(1.0, std::round(0.1 * max_steps)));
+    delay = dm + (1.0 - dm) * std::sin(0.5 * M_PI * phase);
+  }
+  return log_lerp * delay;
+}
+
+// Runs one pass over `nv` cameras.  mode: render / forward (+loss) /
+// backward (gradients out, no Adam) / train (Adam step).
+int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepStats* stats) {
+  if (c->n == 0) return fail(SKY_ERR_STATE, "no Gaussians loaded");
+  if (nv == 0 || nv > (uint32_t)kMaxViews)
+    return fail(SKY_ERR_ARG, "camera count %u outside [1, %d]", nv, kMaxViews);
+  if (inject_launch()) return fail(SKY_ERR_INJECTED, "injected launch failure");
+  const SkyConfig& cfg = c->cfg;
+  const uint32_t ts = cfg.tile_size;
+  const bool with_loss = mode != kRender;
+  StepParams& sp = *c->h_sp;
+  memset(&sp, 0, sizeof(StepParams));
+  // views, tiles, pixels, groups
+  uint64_t tile_total = 0, pix_total = 0;
+  uint32_t max_view_px = 0;
+  uint32_t ngroups = 0;
+  uint64_t group_tiles = 0;
+  for (uint32_t v = 0; v < nv; ++v) {
+    const uint32_t ci = cams[v];
+    if (ci >= c->cams.size()) return fail(SKY_ERR_ARG, "camera %u not set", ci);
+    if (with_loss && !c->tgt_set[ci]) return fail(SKY_ERR_STATE, "camera %u has no target", ci);
+    const SkyCamera& cam = c->cams[ci];
+    ViewInfo& vi = sp.views[v];
+    memcpy(vi.view, cam.view, sizeof(vi.view));
+    memcpy(vi.proj, cam.proj, sizeof(vi.proj));
+    vi.focal[0] = cam.focal[0];
+    vi.focal[1] = cam.focal[1];
+    vi.width = cam.width;
+    vi.height = cam.height;
+    vi.tiles_x = (cam.width + ts - 1) / ts;
+    vi.tiles_y = (cam.height + ts - 1) / ts;
+    const uint64_t vt = (uint64_t)vi.tiles_x * vi.tiles_y;
+    if (vt > 65536)
+      return fail(SKY_ERR_ARG, "camera %u has %llu tiles; at most 65536 per view", ci,
+                  (unsigned long long)vt);
+    if (ngroups == 0 || group_tiles + vt > 65536) {
+      if (ngroups == (uint32_t)kMaxGroups) return fail(SKY_ERR_ARG, "too many sort groups");
+      GroupInfo& g = sp.groups[ngroups];
+      g.tile_begin = (uint32_t)tile_total;
+      g.item_begin = v * c->n;
+      ++ngroups;
+      group_tiles = 0;
+    }
+    GroupInfo& g = sp.groups[ngroups - 1];
+    vi.group = ngroups - 1;
+    vi.key_tile_base = (uint32_t)group_tiles;
+    vi.tile_base = (uint32_t)tile_total;
+    vi.pixel_base = (uint32_t)pix_total;
+    vi.target_base = c->tgt_set[ci] ? (uint32_t)c->tgt_base[ci] : 0u;
+    vi.has_target = c->tgt_set[ci];
+    vi.camera = ci;
+    group_tiles += vt;
+    tile_total += vt;
+    pix_total += (uint64_t)cam.width * cam.height;
+    g.tile_end = (uint32_t)tile_total;
+    g.item_end = (v + 1) * c->n;
+    g.key_bits = 16 + ceil_log2((uint32_t)group_tiles);
+    max_view_px = std::max(max_view_px, cam.width * cam.height);
+  }
+  if (pix_total >= (1ull << 32)) return fail(SKY_ERR_ARG, "too many pixels in one step");
+  const uint64_t items = (uint64_t)nv * c->n;
+  if (items >= (1ull << 32)) return fail(SKY_ERR_ARG, "views x Gaussians exceeds 2^32");
+  // buffers
+  TRY(dev_alloc(c, c->records, items * 48));
+  TRY(dev_alloc(c, c->counts, items * 4));
+  TRY(dev_alloc(c, c->rects, items * 8));
+  TRY(dev_alloc(c, c->cumsum, items * 4));
+  TRY(dev_alloc(c, c->block_sums, (scan_block_count((uint32_t)items) + 1) * 4));
+  TRY(dev_alloc(c, c->offsets, (tile_total + 1) * 4));
+  TRY(dev_alloc(c, c->loss_partials, (tile_total + 1) * 8));
+  TRY(dev_alloc(c, c->color, pix_total * 16));
+  TRY(dev_alloc(c, c->alpha, pix_total * 4));
+  TRY(dev_alloc(c, c->tfinal, pix_total * 4));
+  TRY(dev_alloc(c, c->last, pix_total * 4));
+  TRY(dev_alloc(c, c->residual, pix_total * 16));
+  if (mode == kBackward) TRY(dev_alloc(c, c->grads, (size_t)kPlanes * c->stride * 4));
+  const bool ref = cfg.backward_mode == SKY_BWD_REFERENCE;
+  if (ref && mode >= kBackward) TRY(dev_alloc(c, c->gsum54, items * 54 * 8));
+  if (c->icap == 0) TRY(ensure_isect(c, 1u << 16));
+  // schedules
+  uint64_t it = c->iteration + (mode == kTrain ? 1 : 0);
+  uint32_t deg = cfg.sh_degree;
+  if (cfg.sh_degree_interval > 0)
+    deg = (uint32_t)std::min<uint64_t>(cfg.sh_degree, it / cfg.sh_degree_interval);
+  sp.num_views = nv;
+  sp.n = c->n;
+  sp.num_tiles = (uint32_t)tile_total;
+  sp.num_groups = ngroups;
+  sp.sh_deg = deg;
+  sp.sh_update = (mode == kTrain && cfg.sh_update_interval > 0 && it % cfg.sh_update_interval == 0) ? 1 : 0;
+  sp.bwd_mode = cfg.backward_mode;
+  sp.round_f16 = cfg.round_params_f16;
+  sp.tile_size = ts;
+  sp.has_loss = with_loss ? 1 : 0;
+  sp.apply_adam = mode == kTrain ? 1 : 0;
+  sp.write_grads = mode == kBackward ? 1 : 0;
+  sp.icap = c->icap;
+  sp.num_pixels = (uint32_t)pix_total;
+  sp.plane_stride = c->stride;
+  sp.near_plane = cfg.near_plane;
+  sp.far_plane = cfg.far_plane;
+  sp.radius_clip = cfg.radius_clip;
+  sp.eps2d = cfg.eps2d;
+  for (int k = 0; k < 3; ++k) sp.bg[k] = cfg.background[k];
+  sp.w_l2 = cfg.w_l2;
+  sp.w_l1 = cfg.w_l1;
+  sp.w_ssim = cfg.w_ssim;
+  sp.lr_pos = (float)position_lr(cfg, it);
+  sp.lr_scale = cfg.lr_scale;
+  sp.lr_rot = cfg.lr_rotation;
+  sp.lr_opacity = cfg.lr_opacity;
+  sp.lr_sh = cfg.lr_sh;
+  sp.beta1 = cfg.beta1;
+  sp.beta2 = cfg.beta2;
+  sp.adam_eps = cfg.adam_eps;
+  {
+    // run_adam_on_buffer (gaussian-renderer.ts:2420-2430): t = max(1, counter)
+    const double t = (double)std::max<uint64_t>(1, c->adam_steps);
+    const double bc1 = 1.0 - std::pow(js_literal(cfg.beta1), t);
+    const double bc2 = 1.0 - std::pow(js_literal(cfg.beta2), t);
+    sp.bc1_rcp = (float)(1.0 / bc1);
+    sp.bc2_sqrt_rcp = (float)(1.0 / std::sqrt(bc2));
+  }
+  DevBuffers b = make_buffers(c);
+  cudaStream_t s = c->stream;
+  CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
+  launch_preprocess(b, c->n, nv, s);
+  launch_scan(b, (uint32_t)items, s);
+  launch_group_bounds(b, s);
+  // size the intersection buffers from the device count (the reference reads
+  // the projections back for its host cumsum at the same point)
+  CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (c->h_st->total_isect > c->icap) {
+    TRY(ensure_isect(c, c->h_st->total_isect));
+    b = make_buffers(c);
+    sp.icap = c->icap;
+    CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
+    CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
+    launch_group_bounds(b, s);
+  }
+  launch_emit(b, c->n, nv, s);
+  DevStatus* dst = (DevStatus*)c->d_st.p;
+  for (uint32_t g = 0; g < ngroups; ++g) {
+    SortSegment seg{&dst->group_bounds[g][0], 0};
+    CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap,
+                         sp.groups[g].key_bits, c->sort, &dst->error, s));
+  }
+  launch_ranges(b, c->icap, s);
+  launch_forward(b, (uint32_t)tile_total, ts, with_loss && cfg.w_ssim > 0.0f, nv, max_view_px, s);
+  if (with_loss) launch_loss_final(b, s);
+  if (mode >= kBackward) {
+    if (ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
+    launch_backward(b, (uint32_t)tile_total, ts, ref, s);
+    launch_geom_adam(b, c->n, s);
+  }
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  c->error_flags |= c->h_st->error;
+  if (c->h_st->error & SKY_DEVERR_SORT_TIMEOUT)
+    return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  if (c->h_st->error & SKY_DEVERR_CAPACITY)
+    return fail(SKY_ERR_CAPACITY, "intersection capacity exceeded");
+  c->last_views.assign(cams, cams + nv);
+  c->last_items = (uint32_t)items;
+  c->last_tiles = (uint32_t)tile_total;
+  c->last_pixels = (uint32_t)pix_total;
+  c->last_groups = ngroups;
+  c->last_isect = c->h_st->total_isect;
+  c->last_loss = c->h_st->loss;
+  c->fwd_ready = with_loss;
+  if (mode == kTrain) {
+    c->iteration = it;
+    c->adam_steps += 1;
+  }
+  if (stats) {
+    stats->iteration = c->iteration;
+    stats->num_intersections = c->h_st->total_isect;
+    stats->loss = c->h_st->loss;
+    stats->num_gaussians = c->n;
+    stats->num_views = nv;
+    stats->sh_degree = deg;
+    stats->sh_updated = sp.sh_update;
+  }
+  return SKY_OK;
+}
+
+Context* as_ctx(void* p) { return (Context*)p; }
+
+}  // namespace
+
+// ===========================================================================
+// C-ABI
+// ===========================================================================
+extern "C" {
+
+int sky_version(void) { return 1; }
+
+const char* sky_last_error(void) { return g_err.c_str(); }
+
+void sky_config_default(SkyConfig* c) {
+  if (!c) return;
+  memset(c, 0, sizeof(*c));
+  c->struct_size = sizeof(SkyConfig);
+  c->tile_size = 16;
+  c->sh_degree = 3;
+  c->sh_degree_interval = 1000;
+  c->near_plane = 0.2f;
+  c->far_plane = 10000.0f;
+  c->radius_clip = 512.0f;
+  c->eps2d = 0.3f;
+  c->w_l2 = 0.0f;
+  c->w_l1 = 0.8f;
+  c->w_ssim = 0.2f;
+  c->lr_means = 0.00016f;
+  c->lr_means_final = 0.0000016f;
+  c->lr_means_delay_mult = 0.01f;
+  c->lr_means_max_steps = 30000;
+  c->lr_sh = 0.0025f;
+  c->lr_opacity = 0.025f;
+  c->lr_scale = 0.005f;
+  c->lr_rotation = 0.001f;
+  c->beta1 = 0.9f;
+  c->beta2 = 0.999f;
+  c->adam_eps = 1e-8f;
+  c->sh_update_interval = 16;
+  c->round_params_f16 = 1;
+  c->backward_mode = SKY_BWD_EXACT;
+  c->use_graph = 0;
+  c->max_views_per_step = 16;
+  c->seed = 0x5EEDull;
+}
+
+static int check_cfg(const SkyConfig* cfg) {
+  if (!cfg) return fail(SKY_ERR_ARG, "null config");
+  if (cfg->struct_size != sizeof(SkyConfig))
+    return fail(SKY_ERR_ARG, "SkyConfig size %u, library expects %zu", cfg->struct_size,
+                sizeof(SkyConfig));
+  if (cfg->tile_size != 8 && cfg->tile_size != 16 && cfg->tile_size != 32)
+    return fail(SKY_ERR_ARG, "tile_size %u not in {8, 16, 32}", cfg->tile_size);
+  if (cfg->sh_degree > 3) return fail(SKY_ERR_ARG, "sh_degree %u > 3", cfg->sh_degree);
+  if (cfg->backward_mode > 1) return fail(SKY_ERR_ARG, "unknown backward_mode");
+  return SKY_OK;
+}
+
+int sky_create(const SkyConfig* cfg, void** out) {
+  if (!out) return fail(SKY_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  TRY(check_cfg(cfg));
+  Context* c = new Context();
+  c->cfg = *cfg;
+  c->rng = cfg->seed;
+  int rc = SKY_OK;
+  auto bail = [&](int r) {
+    sky_destroy(c);
+    return r;
+  };
+  cudaError_t e = cudaGetDevice(&c->device);
+  if (e != cudaSuccess) return bail(fail(SKY_ERR_CUDA, "no CUDA device: %s", cudaGetErrorString(e)));
+  e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return bail(fail(SKY_ERR_CUDA, "stream: %s", cudaGetErrorString(e)));
+  e = cudaMallocHost(&c->h_sp, sizeof(StepParams));
+  if (e != cudaSuccess) return bail(fail(SKY_ERR_OOM, "pinned alloc: %s", cudaGetErrorString(e)));
+  e = cudaMallocHost(&c->h_st, sizeof(DevStatus));
+  if (e != cudaSuccess) return bail(fail(SKY_ERR_OOM, "pinned alloc: %s", cudaGetErrorString(e)));
+  if ((rc = dev_alloc(c, c->d_sp, sizeof(StepParams))) != SKY_OK) return bail(rc);
+  if ((rc = dev_alloc(c, c->d_st, sizeof(DevStatus))) != SKY_OK) return bail(rc);
+  *out = c;
+  return SKY_OK;
+}
+
+int sky_destroy(void* p) {
+  Context* c = as_ctx(p);
+  if (!c) return SKY_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records,
+                &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->keys,
+                &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->partials,
+                &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,
+                &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
+                &c->flag_scan, &c->d_sp, &c->d_st};
+  for (Buf* b : all) dev_free(c, *b);
+  if (c->h_sp) cudaFreeHost(c->h_sp);
+  if (c->h_st) cudaFreeHost(c->h_st);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return SKY_OK;
+}
+
+int sky_set_config(void* p, const SkyConfig* cfg) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  TRY(check_cfg(cfg));
+  if (cfg->tile_size != c->cfg.tile_size || cfg->backward_mode != c->cfg.backward_mode)
+    return fail(SKY_ERR_ARG, "tile_size and backward_mode are fixed at creation");
+  c->cfg = *cfg;
+  return SKY_OK;
+}
+
+int sky_camera_pinhole(const float view[16], double fx, double fy, double cx, double cy,
+                       uint32_t width, uint32_t height, SkyCamera* out) {
+  if (!view || !out || width == 0 || height == 0) return fail(SKY_ERR_ARG, "bad camera");
+  memset(out, 0, sizeof(*out));
+  memcpy(out->view, view, 16 * sizeof(float));
+  // get_pinhole_projection_matrix: rows (sx,0,ox,0), (0,sy,oy,0), (0,0,1,0),
+  // (0,0,1,0), stored column-major.
+  const double w = width, h = height;
+  const double sx = 2.0 * fx / w, sy = -2.0 * fy / h;
+  const double ox = 2.0 * cx / w - 1.0, oy = 1.0 - 2.0 * cy / h;
+  float* P = out->proj;
+  P[0 * 4 + 0] = (float)sx;
+  P[1 * 4 + 1] = (float)sy;
+  P[2 * 4 + 0] = (float)ox;
+  P[2 * 4 + 1] = (float)oy;
+  P[2 * 4 + 2] = 1.0f;
+  P[2 * 4 + 3] = 1.0f;
+  out->focal[0] = (float)fx;
+  out->focal[1] = (float)fy;
+  out->width = width;
+  out->height = height;
+  return SKY_OK;
+}
+
+static int load_planes(Context* c, uint32_t n) {
+  uint32_t stride = (n + 255) & ~255u;
+  if (stride == 0) stride = 256;
+  const size_t bytes = (size_t)kPlanes * stride * 4;
+  TRY(dev_alloc(c, c->params, bytes));
+  TRY(dev_alloc(c, c->m1, bytes));
+  TRY(dev_alloc(c, c->m2, bytes));
+  CK(cudaMemsetAsync(c->m1.p, 0, bytes, c->stream));
+  CK(cudaMemsetAsync(c->m2.p, 0, bytes, c->stream));
+  c->n = n;
+  c->stride = stride;
+  c->iteration = 0;
+  c->adam_steps = 0;
+  c->fwd_ready = false;
+  return SKY_OK;
+}
+
+int sky_load_points(void* p, const float* params, uint32_t n, uint64_t plane_stride) {
+  Context* c = as_ctx(p);
+  if (!c || !params || n == 0 || plane_stride < n) return fail(SKY_ERR_ARG, "bad points");
+  TRY(load_planes(c, n));
+  CK(cudaMemcpy2DAsync(c->params.p, (size_t)c->stride * 4, params, (size_t)plane_stride * 4,
+                       (size_t)n * 4, kPlanes, cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return SKY_OK;
+}
+
+static float half_to_float(uint16_t h) {
+  const uint32_t s = (uint32_t)(h & 0x8000u) << 16;
+  uint32_t e = (h >> 10) & 0x1Fu, m = h & 0x3FFu;
+  uint32_t bits;
+  if (e == 0) {
+    if (m == 0) {
+      bits = s;
+    } else {
+      e = 127 - 15 + 1;
+      while (!(m & 0x400u)) {
+        m <<= 1;
+        --e;
+      }
+      m &= 0x3FFu;
+      bits = s | (e << 23) | (m << 13);
+    }
+  } else if (e == 31) {
+    bits = s | 0x7F800000u | (m << 13);
+  } else {
+    bits = s | ((e + 112) << 23) | (m << 13);
+  }
+  float f;
+  memcpy(&f, &bits, 4);
+  return f;
+}
+
+int sky_load_packed(void* p, const uint32_t* gaussians, const uint32_t* sh, uint32_t n) {
+  Context* c = as_ctx(p);
+  if (!c || !gaussians || n == 0) return fail(SKY_ERR_ARG, "bad packed points");
+  // training_init_params (training-params.wgsl:35-79): halves
+  // [x, y | z, opacity | rot0, rot1 | rot2, rot3 | s0, s1 | s2, pad];
+  // train_rotation = (rot1, rot2, rot3, rot0).
+  std::vector<float> planes((size_t)kPlanes * n, 0.0f);
+  for (uint32_t i = 0; i < n; ++i) {
+    const uint16_t* h = (const uint16_t*)(gaussians + (size_t)i * 6);
+    float f[12];
+    for (int k = 0; k < 12; ++k) f[k] = half_to_float(h[k]);
+    const float vals[11] = {f[0], f[1], f[2], f[8], f[9], f[10], f[5], f[6], f[7], f[4], f[3]};
+    for (int k = 0; k < 11; ++k) planes[(size_t)k * n + i] = vals[k];
+    if (sh) {
+      const uint16_t* hs = (const uint16_t*)(sh + (size_t)i * 24);
+      for (int k = 0; k < 48; ++k) planes[(size_t)(11 + k) * n + i] = half_to_float(hs[k]);
+    }
+  }
+  return sky_load_points(p, planes.data(), n, n);
+}
+
+int sky_set_cameras(void* p, const SkyCamera* cams, uint32_t n) {
+  Context* c = as_ctx(p);
+  if (!c || (!cams && n)) return fail(SKY_ERR_ARG, "bad cameras");
+  for (uint32_t i = 0; i < n; ++i)
+    if (cams[i].width == 0 || cams[i].height == 0 || cams[i].focal[0] <= 0 || cams[i].focal[1] <= 0)
+      return fail(SKY_ERR_ARG, "camera %u has an empty image or non-positive focal", i);
+  c->cams.assign(cams, cams + n);
+  c->tgt_base.assign(n, 0);
+  c->tgt_set.assign(n, 0);
+  c->targets_px = 0;
+  c->fwd_ready = false;
+  return SKY_OK;
+}
+
+int sky_set_target(void* p, uint32_t cam, const float* rgb, uint32_t width, uint32_t height) {
+  Context* c = as_ctx(p);
+  if (!c || !rgb) return fail(SKY_ERR_ARG, "bad target");
+  if (cam >= c->cams.size()) return fail(SKY_ERR_ARG, "camera %u not set", cam);
+  if (width != c->cams[cam].width || height != c->cams[cam].height)
+    return fail(SKY_ERR_ARG, "target %ux%u does not match camera %ux%u", width, height,
+                c->cams[cam].width, c->cams[cam].height);
+  const uint64_t px = (uint64_t)width * height;
+  uint64_t base;
+  if (c->tgt_set[cam]) {
+    base = c->tgt_base[cam];
+  } else {
+    base = c->targets_px;
+    if (base + px >= (1ull << 32)) return fail(SKY_ERR_ARG, "target images exceed 2^32 pixels");
+    TRY(dev_alloc(c, c->targets, (base + px) * 16, true));
+    c->targets_px = base + px;
+  }
+  std::vector<float> rgba(px * 4);
+  for (uint64_t i = 0; i < px; ++i) {
+    rgba[i * 4 + 0] = rgb[i * 3 + 0];
+    rgba[i * 4 + 1] = rgb[i * 3 + 1];
+    rgba[i * 4 + 2] = rgb[i * 3 + 2];
+    rgba[i * 4 + 3] = 1.0f;
+  }
+  CK(cudaMemcpyAsync((char*)c->targets.p + base * 16, rgba.data(), px * 16,
+                     cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->tgt_base[cam] = base;
+  c->tgt_set[cam] = 1;
+  return SKY_OK;
+}
+
+int sky_render(void* p, const uint32_t* cams, uint32_t n, float* rgba, float* alpha) {
+  Context* c = as_ctx(p);
+  if (!c || !cams) return fail(SKY_ERR_ARG, "bad render arguments");
+  TRY(run_views(c, cams, n, kRender, nullptr));
+  if (rgba) CK(cudaMemcpy(rgba, c->color.p, (size_t)c->last_pixels * 16, cudaMemcpyDeviceToHost));
+  if (alpha) CK(cudaMemcpy(alpha, c->alpha.p, (size_t)c->last_pixels * 4, cudaMemcpyDeviceToHost));
+  return SKY_OK;
+}
+
+int sky_forward(void* p, const uint32_t* cams, uint32_t n, double* loss) {
+  Context* c = as_ctx(p);
+  if (!c || !cams) return fail(SKY_ERR_ARG, "bad forward arguments");
+  TRY(run_views(c, cams, n, kForward, nullptr));
+  if (loss) *loss = c->last_loss;
+  return SKY_OK;
+}
+
+int sky_backward(void* p, float* grads, uint64_t plane_stride) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (!c->fwd_ready) return fail(SKY_ERR_STATE, "sky_backward needs a preceding sky_forward");
+  std::vector<uint32_t> views = c->last_views;
+  TRY(run_views(c, views.data(), (uint32_t)views.size(), kBackward, nullptr));
+  if (grads) {
+    if (plane_stride < c->n) return fail(SKY_ERR_ARG, "plane_stride < number of Gaussians");
+    CK(cudaMemcpy2D(grads, plane_stride * 4, c->grads.p, (size_t)c->stride * 4, (size_t)c->n * 4,
+                    kPlanes, cudaMemcpyDeviceToHost));
+  }
+  return SKY_OK;
+}
+
+int sky_step(void* p, const uint32_t* cams, uint32_t n, SkyStepStats* stats) {
+  Context* c = as_ctx(p);
+  if (!c || !cams) return fail(SKY_ERR_ARG, "bad step arguments");
+  return run_views(c, cams, n, kTrain, stats);
+}
+
+int sky_train(void* p, uint32_t iterations, uint32_t views_per_step, SkyStepStats* last) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (c->cams.empty()) return fail(SKY_ERR_STATE, "no cameras");
+  if (views_per_step == 0) views_per_step = 1;
+  std::vector<uint32_t> v(views_per_step);
+  for (uint32_t i = 0; i < iterations; ++i) {
+    // Math.floor(Math.random() * numCameras) with a seeded generator
+    for (uint32_t k = 0; k < views_per_step; ++k)
+      v[k] = (uint32_t)(((splitmix64(c->rng) >> 11) * (1.0 / 9007199254740992.0)) * c->cams.size());
+    TRY(run_views(c, v.data(), views_per_step, kTrain, last));
+  }
+  return SKY_OK;
+}
+
+int sky_get_params(void* p, float* out, uint64_t plane_stride) {
+  Context* c = as_ctx(p);
+  if (!c || !out || plane_stride < c->n) return fail(SKY_ERR_ARG, "bad readback");
+  if (c->n == 0) return SKY_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  CK(cudaMemcpy2D(out, plane_stride * 4, c->params.p, (size_t)c->stride * 4, (size_t)c->n * 4,
+                  kPlanes, cudaMemcpyDeviceToHost));
+  return SKY_OK;
+}
+
+int sky_get_moments(void* p, float* m1, float* m2, uint64_t plane_stride) {
+  Context* c = as_ctx(p);
+  if (!c || plane_stride < c->n) return fail(SKY_ERR_ARG, "bad readback");
+  if (c->n == 0) return SKY_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  if (m1)
+    CK(cudaMemcpy2D(m1, plane_stride * 4, c->m1.p, (size_t)c->stride * 4, (size_t)c->n * 4,
+                    kPlanes, cudaMemcpyDeviceToHost));
+  if (m2)
+    CK(cudaMemcpy2D(m2, plane_stride * 4, c->m2.p, (size_t)c->stride * 4, (size_t)c->n * 4,
+                    kPlanes, cudaMemcpyDeviceToHost));
+  return SKY_OK;
+}
+
+int sky_get_count(void* p, uint32_t* n) {
+  Context* c = as_ctx(p);
+  if (!c || !n) return fail(SKY_ERR_ARG, "bad arguments");
+  *n = c->n;
+  return SKY_OK;
+}
+
+int sky_get_status(void* p, SkyStatus* st) {
+  Context* c = as_ctx(p);
+  if (!c || !st) return fail(SKY_ERR_ARG, "bad arguments");
+  memset(st, 0, sizeof(*st));
+  st->iteration = c->iteration;
+  st->adam_steps = c->adam_steps;
+  st->last_intersections = c->last_isect;
+  st->device_bytes = c->device_bytes;
+  st->num_gaussians = c->n;
+  st->capacity = c->stride;
+  st->num_cameras = (uint32_t)c->cams.size();
+  st->error_flags = c->error_flags;
+  return SKY_OK;
+}
+
+int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* size_out) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  const uint64_t items = c->last_items, I = std::min<uint64_t>(c->last_isect, c->icap);
+  const uint64_t T = c->last_tiles, P = c->last_pixels;
+  const void* src = nullptr;
+  uint64_t sz = 0, pitch_src = 0, rows = 0, row_bytes = 0;
+  switch (which) {
+    case SKY_BUF_RECORDS: src = c->records.p; sz = items * 48; break;
+    case SKY_BUF_COUNTS: src = c->counts.p; sz = items * 4; break;
+    case SKY_BUF_CUMSUM: src = c->cumsum.p; sz = items * 4; break;
+    case SKY_BUF_KEYS_EMIT: src = c->keys.p; sz = I * 4; break;
+    case SKY_BUF_KEYS_SORTED: src = c->keys_sorted.p; sz = I * 4; break;
+    case SKY_BUF_VALS_SORTED: src = c->vals_sorted.p; sz = I * 4; break;
+    case SKY_BUF_FLATTEN: src = c->flatten.p; sz = I * 4; break;
+    case SKY_BUF_TILE_OFFSETS: src = c->offsets.p; sz = (T + 1) * 4; break;
+    case SKY_BUF_COLOR: src = c->color.p; sz = P * 16; break;
+    case SKY_BUF_ALPHA: src = c->alpha.p; sz = P * 4; break;
+    case SKY_BUF_LAST_IDS: src = c->last.p; sz = P * 4; break;
+    case SKY_BUF_RESIDUAL: src = c->residual.p; sz = P * 16; break;
+    case SKY_BUF_PARTIALS: src = c->partials.p; sz = I * kPartialF4 * 16; break;
+    case SKY_BUF_TILE_GRADS: src = c->tile_grads.p; sz = c->tile_grads.p ? I * 54 * 4 : 0; break;
+    case SKY_BUF_GRADS:
+      src = c->grads.p;
+      sz = c->grads.p ? (uint64_t)kPlanes * c->n * 4 : 0;
+      pitch_src = (uint64_t)c->stride * 4;
+      rows = kPlanes;
+      row_bytes = (uint64_t)c->n * 4;
+      break;
+    case SKY_BUF_STEP_SCALARS: {
+      const StepParams& q = *c->h_sp;
+      const float v[12] = {q.lr_pos, q.lr_scale, q.lr_rot, q.lr_opacity, q.lr_sh, q.beta1,
+                           q.beta2, q.adam_eps, q.bc1_rcp, q.bc2_sqrt_rcp, (float)q.sh_deg,
+                           (float)q.sh_update};
+      if (size_out) *size_out = sizeof(v);
+      if (dst && bytes >= sizeof(v)) memcpy(dst, v, sizeof(v));
+      return SKY_OK;
+    }
+    case SKY_BUF_GROUPS: {
+      if (size_out) *size_out = (uint64_t)c->last_groups * 8;
+      if (dst && bytes >= (uint64_t)c->last_groups * 8)
+        memcpy(dst, c->h_st->group_bounds, (size_t)c->last_groups * 8);
+      return SKY_OK;
+    }
+    default: return fail(SKY_ERR_ARG, "unknown buffer %d", which);
+  }
+  if (size_out) *size_out = sz;
+  if (!dst || sz == 0) return SKY_OK;
+  if (bytes < sz) return fail(SKY_ERR_ARG, "destination holds %llu bytes, need %llu",
+                              (unsigned long long)bytes, (unsigned long long)sz);
+  CK(cudaStreamSynchronize(c->stream));
+  if (rows)
+    CK(cudaMemcpy2D(dst, row_bytes, src, pitch_src, row_bytes, rows, cudaMemcpyDeviceToHost));
+  else
+    CK(cudaMemcpy(dst, src, sz, cudaMemcpyDeviceToHost));
+  return SKY_OK;
+}
+
+int sky_sync(void* p) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  CK(cudaStreamSynchronize(c->stream));
+  return SKY_OK;
+}
+
+// ---- device-pointer sort ---------------------------------------------------
+static std::mutex g_sort_mu;
+struct SortCache {
+  void* mem = nullptr;
+  size_t bytes = 0;
+  uint32_t max_n = 0;
+  uint32_t* err = nullptr;
+};
+static SortCache g_sort_cache[64];
+
+int sky_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                   uint32_t* vals_out, uint32_t n, uint32_t key_bits, void* stream) {
+  if (!keys_in || !keys_out || !vals_out) return fail(SKY_ERR_ARG, "null device pointer");
+  if (key_bits == 0 || key_bits > 32) return fail(SKY_ERR_ARG, "key_bits %u outside 1..32", key_bits);
+  if (n >= (1u << 30)) return fail(SKY_ERR_ARG, "n = %u exceeds 2^30 - 1", n);
+  if (keys_in == keys_out || (vals_in && vals_in == vals_out))
+    return fail(SKY_ERR_ARG, "input and output arrays must differ");
+  if (n == 0) return SKY_OK;
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return fail(SKY_ERR_ARG, "device index %d unsupported", dev);
+  std::lock_guard<std::mutex> lock(g_sort_mu);
+  SortCache& sc = g_sort_cache[dev];
+  cudaStream_t s = (cudaStream_t)stream;
+  if (n > sc.max_n) {
+    if (sc.mem) {
+      CK(cudaDeviceSynchronize());
+      cudaFree(sc.mem);
+      sc.mem = nullptr;
+    }
+    const size_t bytes = sort_scratch_bytes(n) + 256;
+    if (inject_alloc()) return fail(SKY_ERR_INJECTED, "injected allocation failure");
+    CK(cudaMalloc(&sc.mem, bytes));
+    sc.bytes = bytes;
+    sc.max_n = n;
+    sc.err = (uint32_t*)((char*)sc.mem + bytes - 256);
+  }
+  SortScratch scr = sort_scratch_carve(sc.mem, sc.max_n);
+  CK(cudaMemsetAsync(sc.err, 0, 4, s));
+  SortSegment seg{nullptr, n};
+  CK(sort_pairs_launch(keys_in, vals_in, keys_out, vals_out, seg, n, key_bits, scr, sc.err, s));
+  uint32_t err = 0;
+  CK(cudaMemcpyAsync(&err, sc.err, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (err & SKY_DEVERR_SORT_TIMEOUT) return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  return SKY_OK;
+}
+
+// Not yet implemented entry points report SKY_ERR_STATE.
+int sky_prune(void* p, const SkyPruneParams* prm, const uint8_t* mask, uint32_t* removed);
+int sky_densify_stats(void* p, float* grad_accum, float* importance) {
+  (void)p; (void)grad_accum; (void)importance;
+  return fail(SKY_ERR_STATE, "densify statistics are not implemented");
+}
+int sky_densify(void* p, const SkyDensifyParams* prm, uint32_t* cloned, uint32_t* split) {
+  (void)p; (void)prm; (void)cloned; (void)split;
+  return fail(SKY_ERR_STATE, "densify is not implemented");
+}
+int sky_reset_opacity(void* p, float max_opacity);
+
+}  // extern "C"
+
+// ---- prune / opacity reset (compact.cu kernels) ---------------------------
+extern "C" int sky_prune(void* p, const SkyPruneParams* prm, const uint8_t* mask,
+                         uint32_t* removed) {
+  Context* c = as_ctx(p);
+  if (removed) *removed = 0;
+  if (!c || (!prm && !mask)) return fail(SKY_ERR_ARG, "bad prune arguments");
+  if (c->n == 0) return SKY_OK;
+  const uint32_t n = c->n;
+  cudaStream_t s = c->stream;
+  Buf dmask;
+  if (mask) {
+    TRY(dev_alloc(c, dmask, n));
+    CK(cudaMemcpyAsync(dmask.p, mask, n, cudaMemcpyHostToDevice, s));
+  }
+  TRY(dev_alloc(c, c->flags, (size_t)n * 4));
+  TRY(dev_alloc(c, c->flag_scan, (size_t)n * 4));
+  TRY(dev_alloc(c, c->block_sums, (scan_block_count(n) + 1) * 4));
+  const float min_op = prm ? prm->min_opacity : 0.0f;
+  const float max_scale = prm ? prm->max_scale : INFINITY;
+  launch_prune_flags((const float*)c->params.p, c->stride, n, min_op, max_scale,
+                     (const uint8_t*)dmask.p, (uint32_t*)c->flags.p, s);
+  // flags hold 1 for survivors; optional cap on the removal count
+  std::vector<uint32_t> keep(n);
+  CK(cudaMemcpyAsync(keep.data(), c->flags.p, (size_t)n * 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (dmask.p) dev_free(c, dmask);
+  uint64_t remove = 0;
+  for (uint32_t i = 0; i < n; ++i) remove += keep[i] == 0;
+  if (prm && prm->max_remove_ratio > 0.0f && remove > 0) {
+    const uint64_t cap = std::max<uint64_t>(1, (uint64_t)std::floor(n * (double)prm->max_remove_ratio));
+    if (remove > cap) {
+      uint64_t seen = 0;
+      for (uint32_t i = 0; i < n; ++i)
+        if (keep[i] == 0 && ++seen > cap) keep[i] = 1;
+      remove = cap;
+      CK(cudaMemcpyAsync(c->flags.p, keep.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s));
+    }
+  }
+  // applyPruneMask (gaussian-renderer.ts:2917-2925): nothing to do when no
+  // Gaussian or every Gaussian would be removed.
+  if (remove == 0 || remove >= n) return SKY_OK;
+  DevBuffers sb{};
+  sb.counts = (uint32_t*)c->flags.p;
+  sb.cumsum = (uint32_t*)c->flag_scan.p;
+  sb.block_sums = (uint32_t*)c->block_sums.p;
+  launch_scan(sb, n, s);
+  const uint32_t keep_n = (uint32_t)(n - remove);
+  uint32_t new_stride = (keep_n + 255) & ~255u;
+  const size_t bytes = (size_t)kPlanes * new_stride * 4;
+  Buf* planes[3] = {&c->params, &c->m1, &c->m2};
+  for (Buf* pl : planes) {
+    Buf nb;
+    TRY(dev_alloc(c, nb, bytes));
+    launch_compact((const float*)pl->p, (float*)nb.p, c->stride, new_stride, kPlanes, n,
+                   (const uint32_t*)c->flag_scan.p, s);
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    dev_free(c, *pl);
+    *pl = nb;
+  }
+  if (c->grads.p) dev_free(c, c->grads);
+  c->n = keep_n;
+  c->stride = new_stride;
+  c->fwd_ready = false;
+  if (removed) *removed = (uint32_t)remove;
+  return SKY_OK;
+}
+
+extern "C" int sky_reset_opacity(void* p, float max_opacity) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (!(max_opacity > 0.0f && max_opacity < 1.0f)) return fail(SKY_ERR_ARG, "max_opacity outside (0, 1)");
+  if (c->n == 0) return SKY_OK;
+  const float logit = (float)std::log((double)max_opacity / (1.0 - (double)max_opacity));
+  launch_reset_opacity((float*)c->params.p, c->stride, c->n, logit, c->stream);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return SKY_OK;
+}

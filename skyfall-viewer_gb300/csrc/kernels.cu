@@ -1,0 +1,1082 @@
+// Hot-path kernels of the skyfall library: preprocess, scan, key emission,
+// tile ranges, the tiled forward rasterizer with the fused loss, the tiled
+// backward (exact and reference modes), and the fused geometry adjoint +
+// Adam.  Sort lives in sort.cu.  See kernels.cuh for the launch interface.
+#include "kernels.cuh"
+#include "project.cuh"
+
+namespace sky {
+namespace {
+
+constexpr uint32_t kFull = 0xFFFFFFFFu;
+
+SKY_DEV float load_plane(const float* __restrict__ P, uint32_t stride, int plane, uint32_t g,
+                         bool r16) {
+  float v = __ldg(&P[(size_t)plane * stride + g]);
+  return r16 ? round_f16(v) : v;
+}
+
+SKY_DEV float load_plane_rw(const float* P, uint32_t stride, int plane, uint32_t g, bool r16) {
+  float v = P[(size_t)plane * stride + g];
+  return r16 ? round_f16(v) : v;
+}
+
+SKY_DEV int find_view(const StepParams& sp, uint32_t tile) {
+  int v = 0;
+  for (int k = 1; k < (int)sp.num_views; ++k)
+    if (sp.views[k].tile_base <= tile) v = k;
+  return v;
+}
+
+SKY_DEV bool capacity_failed(const DevStatus* st) {
+  return (*(volatile const uint32_t*)&st->error & SKY_DEVERR_CAPACITY) != 0u;
+}
+
+// ---------------------------------------------------------------------------
+// Preprocess: one thread per (view, Gaussian) item.  Grid (ceil(N/256), V).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_preprocess(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t v = blockIdx.y;
+  if (g >= sp.n || v >= sp.num_views) return;
+  const ViewInfo& vi = sp.views[v];
+  const bool r16 = sp.round_f16 != 0;
+  const uint32_t stride = sp.plane_stride;
+  auto get = [&](int plane) { return load_plane(b.params, stride, plane, g, r16); };
+  ProjOut o;
+  const bool ok = project_gaussian(get, vi, sp, (int)sp.sh_deg, true, o);
+  const size_t item = (size_t)v * sp.n + g;
+  // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
+  // whatever the rounding of exp, so skipping it there decides as the
+  // reference does.
+  float smax = -1.0f;
+  if (ok) smax = __logf(255.0f * o.opacity) + 1e-3f;
+  float4* rec = b.records + item * 3;
+  rec[0] = make_float4(o.mx, o.my, o.ca, o.cb);
+  rec[1] = make_float4(o.cc, o.opacity, o.col[0], o.col[1]);
+  rec[2] = make_float4(o.col[2], o.depth, o.radius, smax);
+  b.counts[item] = o.count;
+  b.rects[item] = make_uint2(o.x0 | (o.y0 << 16), o.x1 | (o.y1 << 16));
+}
+
+// ---------------------------------------------------------------------------
+// Scan of the tile counts (reduce, scan of block sums, scan + add).
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 256;
+constexpr int kScanItems = 16;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+SKY_DEV uint32_t block_excl_scan(uint32_t x, uint32_t* s_warp, uint32_t& total) {
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t y = x;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t t = __shfl_up_sync(kFull, y, o);
+    if (lane >= (uint32_t)o) y += t;
+  }
+  if (lane == 31) s_warp[warp] = y;
+  __syncthreads();
+  uint32_t add = 0, tot = 0;
+  const uint32_t nw = blockDim.x >> 5;
+  for (uint32_t w = 0; w < nw; ++w) {
+    if (w < warp) add += s_warp[w];
+    tot += s_warp[w];
+  }
+  total = tot;
+  __syncthreads();
+  return y - x + add;
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevBuffers b, uint32_t n_items) {
+  __shared__ uint32_t s_warp[kScanThreads / 32];
+  const uint32_t base = blockIdx.x * kScanTile;
+  uint32_t sum = 0;
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t i = base + k * kScanThreads + threadIdx.x;
+    if (i < n_items) sum += b.counts[i];
+  }
+  uint32_t total;
+  block_excl_scan(sum, s_warp, total);
+  if (threadIdx.x == 0) b.block_sums[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_scan_blocks(DevBuffers b, uint32_t nblocks) {
+  __shared__ uint32_t s_warp[32];
+  uint32_t carry = 0;
+  for (uint32_t base = 0; base < nblocks; base += 1024) {
+    uint32_t i = base + threadIdx.x;
+    uint32_t v = i < nblocks ? b.block_sums[i] : 0u;
+    uint32_t total;
+    uint32_t ex = block_excl_scan(v, s_warp, total);
+    if (i < nblocks) b.block_sums[i] = carry + ex;
+    carry += total;
+  }
+}
+
+__global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint32_t n_items) {
+  __shared__ uint32_t s_warp[kScanThreads / 32];
+  const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+  uint32_t v[kScanItems];
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    uint32_t i = base + k;
+    v[k] = i < n_items ? b.counts[i] : 0u;
+    sum += v[k];
+  }
+  uint32_t total;
+  uint32_t run = block_excl_scan(sum, s_warp, total) + b.block_sums[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < kScanItems; ++k) {
+    run += v[k];
+    uint32_t i = base + k;
+    if (i < n_items) b.cumsum[i] = run;
+  }
+}
+
+// Group bounds of the sort segments and the capacity check.
+__global__ void k_group_bounds(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  const uint32_t items = sp.num_views * sp.n;
+  const uint32_t total = items ? b.cumsum[items - 1] : 0u;
+  if (threadIdx.x == 0) {
+    b.status->total_isect = total;
+    if (total > sp.icap) atomicOr(&b.status->error, SKY_DEVERR_CAPACITY);
+  }
+  for (uint32_t g = threadIdx.x; g < sp.num_groups; g += blockDim.x) {
+    const GroupInfo& gi = sp.groups[g];
+    uint32_t lo = gi.item_begin ? b.cumsum[gi.item_begin - 1] : 0u;
+    uint32_t hi = gi.item_end ? b.cumsum[gi.item_end - 1] : 0u;
+    b.status->group_bounds[g][0] = min(lo, sp.icap);
+    b.status->group_bounds[g][1] = min(hi, sp.icap);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Key emission: (key_tile << 16) | depth16 in row-major tile order per item,
+// items in (view, Gaussian) order -- emit_intersections
+// (training-tiles.wgsl:265-311) with a per-group tile field.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t v = blockIdx.y;
+  if (g >= sp.n || v >= sp.num_views) return;
+  const size_t item = (size_t)v * sp.n + g;
+  const uint32_t cnt = b.counts[item];
+  if (cnt == 0) return;
+  const uint32_t end = b.cumsum[item];
+  if (end > sp.icap) return;
+  uint32_t cur = end - cnt;
+  const ViewInfo& vi = sp.views[v];
+  const uint2 rc = b.rects[item];
+  const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
+  const float depth = b.records[item * 3 + 2].y;
+  const uint32_t dq = wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
+  const uint32_t it = (uint32_t)item;
+  for (uint32_t ty = y0; ty < y1; ++ty)
+    for (uint32_t tx = x0; tx < x1; ++tx) {
+      const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
+      b.keys[cur] = (kt << 16) | dq;
+      b.rec_of[cur] = it;
+      ++cur;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Tile ranges: offsets[t] = first sorted intersection of tile t, empty tiles
+// take the start of the next non-empty one (build_tile_offsets +
+// host backward min-fill, training-tiles.wgsl:313-335 and
+// gaussian-renderer.ts:1966-2020).  Also resolves the item of every sorted
+// intersection.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  if (capacity_failed(b.status)) return;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t total = min(b.status->total_isect, sp.icap);
+  if (i >= total) return;
+  int g = 0;
+  for (int k = 0; k < (int)sp.num_groups; ++k)
+    if (b.status->group_bounds[k][0] <= i && i < b.status->group_bounds[k][1]) g = k;
+  const GroupInfo& gi = sp.groups[g];
+  const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
+  const uint32_t t = gi.tile_begin + (b.keys_sorted[i] >> 16);
+  if (i == gb) {
+    for (uint32_t u = gi.tile_begin; u <= t; ++u) b.offsets[u] = i;
+  } else {
+    const uint32_t tp = gi.tile_begin + (b.keys_sorted[i - 1] >> 16);
+    for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
+  }
+  if (i + 1 == ge)
+    for (uint32_t u = t + 1; u < gi.tile_end; ++u) b.offsets[u] = ge;
+  b.flatten[i] = b.rec_of[b.vals_sorted[i]];
+}
+
+// Empty groups and the final sentinel offsets[num_tiles] = total.
+__global__ void k_ranges_empty(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  if (capacity_failed(b.status)) return;
+  for (uint32_t g = 0; g < sp.num_groups; ++g) {
+    const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
+    if (gb != ge) continue;
+    const GroupInfo& gi = sp.groups[g];
+    for (uint32_t u = gi.tile_begin + threadIdx.x; u < gi.tile_end; u += blockDim.x)
+      b.offsets[u] = gb;
+  }
+  if (threadIdx.x == 0) b.offsets[sp.num_tiles] = min(b.status->total_isect, sp.icap);
+}
+
+// ---------------------------------------------------------------------------
+// Forward: training_tiled_forward (training-forward-tiles.wgsl:107-215), one
+// CTA per tile, one thread per pixel, splat records staged in shared memory
+// one batch of TS*TS at a time, whole-CTA early exit once every pixel has
+// reached the transmittance threshold.  The loss of training-loss.wgsl:86-126
+// (without its SSIM term) is fused into the epilogue.
+// ---------------------------------------------------------------------------
+constexpr int kFwdBatch = 256;
+
+template <int TS>
+__global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
+  constexpr int NT = TS * TS;
+  __shared__ float4 s_rec[kFwdBatch * 3];
+  __shared__ double s_loss[NT / 32];
+  const StepParams& sp = *b.sp;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= sp.num_tiles) return;
+  if (capacity_failed(b.status)) return;
+  const int v = find_view(sp, tile);
+  const ViewInfo& vi = sp.views[v];
+  const uint32_t local = tile - vi.tile_base;
+  const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
+  const uint32_t tid = threadIdx.x;
+  const uint32_t x = tx * TS + (tid % TS), y = ty * TS + (tid / TS);
+  const bool inside = x < vi.width && y < vi.height;
+  const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
+  const float pxf = (float)x + 0.5f, pyf = (float)y + 0.5f;
+  float C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, A = 0.0f, Tp = 1.0f;
+  uint32_t last = start;
+  bool done = !inside;
+  for (uint32_t bs = start; bs < end; bs += kFwdBatch) {
+    const uint32_t cnt = min((uint32_t)kFwdBatch, end - bs);
+    __syncthreads();
+    for (uint32_t k = tid; k < cnt; k += NT) {
+      const size_t r = b.flatten[bs + k];
+      s_rec[k * 3 + 0] = b.records[r * 3 + 0];
+      s_rec[k * 3 + 1] = b.records[r * 3 + 1];
+      s_rec[k * 3 + 2] = b.records[r * 3 + 2];
+    }
+    __syncthreads();
+    if (!done) {
+      for (uint32_t j = 0; j < cnt; ++j) {
+        last = bs + j;
+        const float4 r0 = s_rec[j * 3 + 0];
+        const float4 r2 = s_rec[j * 3 + 2];
+        const float dx = pxf - r0.x, dy = pyf - r0.y;
+        const float s1 = (r0.z * dx) * dx;
+        const float4 r1 = s_rec[j * 3 + 1];
+        const float s2 = (r1.x * dy) * dy;
+        float so2 = 0.5f * (s1 + s2);
+        so2 = so2 + (r0.w * dx) * dy;
+        if (so2 < 0.0f || so2 > r2.w) continue;
+        const float G = sky_expf(-so2);
+        const float al = r1.y * G;
+        const float a = fmin_(al, MAX_ALPHA);
+        if (a < MIN_ALPHA) continue;
+        const float om = 1.0f - A;
+        const float ca = a * om;
+        C0 = C0 + r1.z * ca;
+        C1 = C1 + r1.w * ca;
+        C2 = C2 + r2.x * ca;
+        A = A + ca;
+        Tp = Tp * (1.0f - a);
+        if (1.0f - A < T_THRESH) {
+          done = true;
+          break;
+        }
+      }
+    }
+    if (__syncthreads_and(done)) break;
+  }
+  double lpx = 0.0;
+  if (inside) {
+    const size_t p = (size_t)vi.pixel_base + (size_t)y * vi.width + x;
+    const float T = 1.0f - A;
+    const float o0 = C0 + T * sp.bg[0], o1 = C1 + T * sp.bg[1], o2 = C2 + T * sp.bg[2];
+    if (start >= end) last = 0xFFFFFFFFu;
+    b.color[p] = make_float4(o0, o1, o2, 1.0f);
+    b.alpha[p] = A;
+    b.tfinal[p] = Tp;
+    b.last[p] = last;
+    if (sp.has_loss && vi.has_target) {
+      const float4 tg = b.targets[(size_t)vi.target_base + (size_t)y * vi.width + x];
+      const float d0 = o0 - tg.x, d1 = o1 - tg.y, d2 = o2 - tg.z;
+      auto sgn = [](float d) { return d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f); };
+      const float g0 = sp.w_l2 * d0 + sp.w_l1 * sgn(d0);
+      const float g1 = sp.w_l2 * d1 + sp.w_l1 * sgn(d1);
+      const float g2 = sp.w_l2 * d2 + sp.w_l1 * sgn(d2);
+      b.residual[p] = make_float4(g0, g1, g2, 0.0f);
+      const double hl2 = 0.5 * (double)sp.w_l2, wl1 = (double)sp.w_l1;
+      lpx = hl2 * (double)d0 * (double)d0 + wl1 * fabs((double)d0);
+      lpx += hl2 * (double)d1 * (double)d1 + wl1 * fabs((double)d1);
+      lpx += hl2 * (double)d2 * (double)d2 + wl1 * fabs((double)d2);
+    }
+  }
+  if (sp.has_loss) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) lpx += __shfl_xor_sync(kFull, lpx, o);
+    if ((tid & 31) == 0) s_loss[tid >> 5] = lpx;
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0;
+      for (int w = 0; w < NT / 32; ++w) s += s_loss[w];
+      b.loss_partials[tile] = s;
+    }
+  }
+}
+
+// SSIM pseudo-gradient term (training-loss.wgsl:33-84), added to the
+// residual after the forward when w_ssim > 0.  One thread per pixel of the
+// step (grid-stride over views).
+__global__ void __launch_bounds__(256) k_ssim(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  if (capacity_failed(b.status)) return;
+  const uint32_t v = blockIdx.y;
+  if (v >= sp.num_views) return;
+  const ViewInfo& vi = sp.views[v];
+  if (!vi.has_target) return;
+  const uint32_t np = vi.width * vi.height;
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= np) return;
+  const int W = (int)vi.width, H = (int)vi.height;
+  const int x = (int)(i % vi.width), y = (int)(i / vi.width);
+  auto P = [&](int xx, int yy) {
+    xx = min(max(xx, 0), W - 1);
+    yy = min(max(yy, 0), H - 1);
+    return b.color[(size_t)vi.pixel_base + (size_t)yy * W + xx];
+  };
+  auto Tg = [&](int xx, int yy) {
+    xx = min(max(xx, 0), W - 1);
+    yy = min(max(yy, 0), H - 1);
+    return b.targets[(size_t)vi.target_base + (size_t)yy * W + xx];
+  };
+  const float C1 = 0.01f * 0.01f, C2 = 0.03f * 0.03f, nwin = 25.0f;
+  float out[3];
+  for (int c = 0; c < 3; ++c) {
+    auto comp = [c](float4 f) { return c == 0 ? f.x : (c == 1 ? f.y : f.z); };
+    float mx = 0.0f, my = 0.0f;
+    for (int dy = -2; dy <= 2; ++dy)
+      for (int dx = -2; dx <= 2; ++dx) {
+        mx = mx + comp(P(x + dx, y + dy));
+        my = my + comp(Tg(x + dx, y + dy));
+      }
+    mx = mx / nwin;
+    my = my / nwin;
+    float sx = 0.0f, sy = 0.0f, sxy = 0.0f;
+    for (int dy = -2; dy <= 2; ++dy)
+      for (int dx = -2; dx <= 2; ++dx) {
+        float a = comp(P(x + dx, y + dy)) - mx;
+        float bb = comp(Tg(x + dx, y + dy)) - my;
+        sx = sx + a * a;
+        sy = sy + bb * bb;
+        sxy = sxy + a * bb;
+      }
+    sx = sx / nwin;
+    sy = sy / nwin;
+    sxy = sxy / nwin;
+    float num1 = (2.0f * mx) * my + C1;
+    float num2 = 2.0f * sxy + C2;
+    float den1 = (mx * mx + my * my) + C1;
+    float den2 = (sx + sy) + C2;
+    float ssim = (num1 * num2) / (den1 * den2);
+    float dssim = (1.0f - ssim) * 0.5f;
+    out[c] = dssim * (comp(P(x, y)) - comp(Tg(x, y)));
+  }
+  const size_t p = (size_t)vi.pixel_base + i;
+  float4 r = b.residual[p];
+  r.x = r.x + sp.w_ssim * out[0];
+  r.y = r.y + sp.w_ssim * out[1];
+  r.z = r.z + sp.w_ssim * out[2];
+  b.residual[p] = r;
+}
+
+__global__ void __launch_bounds__(1024) k_loss_final(DevBuffers b) {
+  __shared__ double s[32];
+  const StepParams& sp = *b.sp;
+  double acc = 0.0;
+  // fixed assignment of tiles to threads, then a fixed tree
+  for (uint32_t t = threadIdx.x; t < sp.num_tiles; t += blockDim.x) acc += b.loss_partials[t];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s[w];
+    b.status->loss = t;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Backward, exact mode.  One CTA per tile; each pixel walks its composited
+// splats back to front from its last contributor, recomputing transmittance
+// from the final product transmittance (T_before = T / (1 - alpha); the
+// product keeps relative precision where 1 - alpha_final would cancel); per
+// pair it forms the
+// nine quantities of backward-tiles-local.wgsl:333-359 (dL/dcolour replaces
+// the 48 SH products: the SH chain is applied once per Gaussian later).
+// Each batch's per-pair values are reduced over the warp with a fixed
+// butterfly, then over the warps in index order, and written per
+// intersection to partials[emission index] -- so every Gaussian's partials
+// are contiguous and the later per-Gaussian sum has a fixed order.
+// ---------------------------------------------------------------------------
+template <int TS>
+__global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
+  constexpr int NT = TS * TS;
+  constexpr int NW = NT / 32;
+  constexpr int kBwdBatch = NW <= 8 ? 64 : 16;
+  __shared__ float4 s_rec[kBwdBatch * 3];
+  __shared__ float s_part[NW][kBwdBatch][9];
+  __shared__ int s_hi[NW];
+  const StepParams& sp = *b.sp;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= sp.num_tiles) return;
+  if (capacity_failed(b.status)) return;
+  const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
+  if (start >= end) return;
+  const int v = find_view(sp, tile);
+  const ViewInfo& vi = sp.views[v];
+  const uint32_t local = tile - vi.tile_base;
+  const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t x = tx * TS + (tid % TS), y = ty * TS + (tid / TS);
+  const bool inside = x < vi.width && y < vi.height;
+  float T = 1.0f, acc0 = sp.bg[0], acc1 = sp.bg[1], acc2 = sp.bg[2];
+  float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+  int myhi = (int)start - 1;
+  const float pxf = (float)x + 0.5f, pyf = (float)y + 0.5f;
+  if (inside) {
+    const size_t p = (size_t)vi.pixel_base + (size_t)y * vi.width + x;
+    const uint32_t lst = b.last[p];
+    if (lst >= start) myhi = (int)min(lst, end - 1);
+    T = b.tfinal[p];
+    const float4 rs = b.residual[p];
+    r0 = rs.x; r1 = rs.y; r2 = rs.z;
+  }
+  int hi = myhi;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) hi = max(hi, __shfl_xor_sync(kFull, hi, o));
+  if (lane == 0) s_hi[warp] = hi;
+  __syncthreads();
+  hi = s_hi[0];
+  for (int w = 1; w < NW; ++w) hi = max(hi, s_hi[w]);
+  // intersections no pixel reaches get zero partials
+  for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
+    float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
+    dst[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    dst[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    dst[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int bhi = hi; bhi >= (int)start; bhi -= kBwdBatch) {
+    const int cnt = min(kBwdBatch, bhi - (int)start + 1);
+    __syncthreads();
+    for (int k = (int)tid; k < cnt; k += NT) {
+      const size_t r = b.flatten[bhi - k];
+      s_rec[k * 3 + 0] = b.records[r * 3 + 0];
+      s_rec[k * 3 + 1] = b.records[r * 3 + 1];
+      s_rec[k * 3 + 2] = b.records[r * 3 + 2];
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      const int i = bhi - j;
+      float val[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) val[k] = 0.0f;
+      bool contrib = false;
+      if (i <= myhi) {
+        const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1], q2 = s_rec[j * 3 + 2];
+        const float dx = pxf - q0.x, dy = pyf - q0.y;
+        const float s1 = (q0.z * dx) * dx;
+        const float s2 = (q1.x * dy) * dy;
+        float so2 = 0.5f * (s1 + s2);
+        so2 = so2 + (q0.w * dx) * dy;
+        if (so2 >= 0.0f && so2 <= q2.w) {
+          const float G = sky_expf(-so2);
+          const float op = q1.y;
+          const float al = op * G;
+          const float a = fmin_(al, MAX_ALPHA);
+          if (a >= MIN_ALPHA) {
+            contrib = true;
+            const float cr = q1.z, cg = q1.w, cbl = q2.x;
+            const float om = fmax_(1.0f - a, 0.0001f);
+            const float Tb = T / om;
+            const float ctb = a * Tb;
+            float fg = r0 * cr + r1 * cg;
+            fg = fg + r2 * cbl;
+            float bgt = r0 * acc0 + r1 * acc1;
+            bgt = bgt + r2 * acc2;
+            const float dLda = (fg - bgt) * Tb;
+            float dlogit = (dLda * a) * (1.0f - op);
+            float dLdG = dLda * op;
+            if (al > MAX_ALPHA) {
+              dlogit = 0.0f;
+              dLdG = 0.0f;
+            }
+            const float dLds = dLdG * (-G);
+            val[0] = r0 * ctb;
+            val[1] = r1 * ctb;
+            val[2] = r2 * ctb;
+            val[3] = dlogit;
+            val[4] = ((dLds * 0.5f) * dx) * dx;
+            val[5] = (dLds * dx) * dy;
+            val[6] = ((dLds * 0.5f) * dy) * dy;
+            val[7] = -(dLds * ((q0.z * dx) + (q0.w * dy)));
+            val[8] = -(dLds * ((q0.w * dx) + (q1.x * dy)));
+            acc0 = a * cr + (1.0f - a) * acc0;
+            acc1 = a * cg + (1.0f - a) * acc1;
+            acc2 = a * cbl + (1.0f - a) * acc2;
+            T = Tb;
+          }
+        }
+      }
+      if (__any_sync(kFull, contrib)) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) {
+          float s = val[k];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(kFull, s, o);
+          val[k] = s;
+        }
+      }
+      if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 9; ++k) s_part[warp][j][k] = val[k];
+      }
+    }
+    __syncthreads();
+    for (int j = (int)tid; j < cnt; j += NT) {
+      float sum[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) sum[k] = s_part[0][j][k];
+      for (int w = 1; w < NW; ++w)
+#pragma unroll
+        for (int k = 0; k < 9; ++k) sum[k] = sum[k] + s_part[w][j][k];
+      float4* dst = b.partials + (size_t)b.vals_sorted[bhi - j] * kPartialF4;
+      dst[0] = make_float4(sum[0], sum[1], sum[2], sum[3]);
+      dst[1] = make_float4(sum[4], sum[5], sum[6], sum[7]);
+      dst[2] = make_float4(sum[8], 0.0f, 0.0f, 0.0f);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Backward, reference mode: backward-tiles-local.wgsl:185-382 as written --
+// batches of 64 intersections in ascending order, each walked back to front
+// per pixel, alpha > 0.98 skipped, 54 values per pair truncated to i32 fixed
+// point (x65536) and summed per (tile, intersection); then per item the 54
+// sums are added exactly in i64 (backward-reduce.wgsl:35-71 without its
+// order-dependent float CAS).
+// ---------------------------------------------------------------------------
+constexpr int kRefBatch = 64;
+
+template <int TS>
+__global__ void __launch_bounds__(TS* TS) k_backward_ref(DevBuffers b) {
+  constexpr int NT = TS * TS;
+  __shared__ float4 s_rec[kRefBatch * 3];
+  __shared__ float s_dir[kRefBatch * 3];
+  __shared__ int s_tg[kRefBatch][54];
+  const StepParams& sp = *b.sp;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= sp.num_tiles) return;
+  if (capacity_failed(b.status)) return;
+  const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
+  if (start >= end) return;
+  const int v = find_view(sp, tile);
+  const ViewInfo& vi = sp.views[v];
+  const uint32_t local = tile - vi.tile_base;
+  const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31;
+  const uint32_t x = tx * TS + (tid % TS), y = ty * TS + (tid / TS);
+  const bool inside = x < vi.width && y < vi.height;
+  const int deg = (int)sp.sh_deg;
+  float T = 1.0f, acc0 = sp.bg[0], acc1 = sp.bg[1], acc2 = sp.bg[2];
+  float r0 = 0.0f, r1 = 0.0f, r2 = 0.0f;
+  uint32_t binf = 0;
+  bool valid = false;
+  const float pxf = (float)x + 0.5f, pyf = (float)y + 0.5f;
+  if (inside) {
+    const size_t p = (size_t)vi.pixel_base + (size_t)y * vi.width + x;
+    binf = b.last[p];
+    T = 1.0f - b.alpha[p];
+    const float4 rs = b.residual[p];
+    r0 = rs.x; r1 = rs.y; r2 = rs.z;
+    valid = binf >= start && binf != 0xFFFFFFFFu;
+  }
+  const bool r16 = sp.round_f16 != 0;
+  for (uint32_t bs = start; bs < end; bs += kRefBatch) {
+    const uint32_t be = min(bs + kRefBatch, end);
+    const int cnt = (int)(be - bs);
+    __syncthreads();
+    for (int k = tid; k < kRefBatch * 54; k += NT) (&s_tg[0][0])[k] = 0;
+    if ((int)tid < cnt) {
+      const size_t r = b.flatten[bs + tid];
+      s_rec[tid * 3 + 0] = b.records[r * 3 + 0];
+      s_rec[tid * 3 + 1] = b.records[r * 3 + 1];
+      s_rec[tid * 3 + 2] = b.records[r * 3 + 2];
+      // view direction normalize(-(view * p)), as the projection computes it
+      const uint32_t g = (uint32_t)(r % sp.n);
+      const float px = load_plane(b.params, sp.plane_stride, 0, g, r16);
+      const float py = load_plane(b.params, sp.plane_stride, 1, g, r16);
+      const float pz = load_plane(b.params, sp.plane_stride, 2, g, r16);
+      const float c0 = -mat4_row(vi.view, 0, px, py, pz, 1.0f);
+      const float c1 = -mat4_row(vi.view, 1, px, py, pz, 1.0f);
+      const float c2 = -mat4_row(vi.view, 2, px, py, pz, 1.0f);
+      float vv = c0 * c0 + c1 * c1;
+      vv = vv + c2 * c2;
+      const float vl = sqrtf(vv);
+      s_dir[tid * 3 + 0] = c0 / vl;
+      s_dir[tid * 3 + 1] = c1 / vl;
+      s_dir[tid * 3 + 2] = c2 / vl;
+    }
+    __syncthreads();
+    const uint32_t pe = valid ? min(be, binf + 1) : bs;
+    for (int jj = cnt - 1; jj >= 0; --jj) {
+      const uint32_t i = bs + (uint32_t)jj;
+      int val[54];
+#pragma unroll
+      for (int k = 0; k < 54; ++k) val[k] = 0;
+      bool contrib = false;
+      if (i < pe) {
+        const float4 q0 = s_rec[jj * 3 + 0], q1 = s_rec[jj * 3 + 1], q2 = s_rec[jj * 3 + 2];
+        const float dx = pxf - q0.x, dy = pyf - q0.y;
+        const float s1 = (q0.z * dx) * dx;
+        const float s2 = (q1.x * dy) * dy;
+        float so2 = 0.5f * (s1 + s2);
+        so2 = so2 + (q0.w * dx) * dy;
+        if (so2 >= 0.0f && so2 <= q2.w) {
+          const float G = sky_expf(-so2);
+          const float op = q1.y;
+          const float a = fmin_(op * G, MAX_ALPHA);
+          if (a >= MIN_ALPHA && !(a > 0.98f)) {
+            contrib = true;
+            const float cr = q1.z, cg = q1.w, cbl = q2.x;
+            const float om = fmax_(1.0f - a, 0.0001f);
+            const float Tb = T / om;
+            const float ctb = a * Tb;
+            const float rs0 = r0 * ctb, rs1 = r1 * ctb, rs2 = r2 * ctb;
+            const float xd = s_dir[jj * 3 + 0], yd = s_dir[jj * 3 + 1], zd = s_dir[jj * 3 + 2];
+            float Y[16];
+            sh_basis(xd, yd, zd, deg, Y);
+            const int ncoef = (deg + 1) * (deg + 1);
+#pragma unroll
+            for (int k = 0; k < 16; ++k) {
+              if (k < ncoef) {
+                val[6 + 3 * k + 0] = wgsl_i32((Y[k] * rs0) * 65536.0f);
+                val[6 + 3 * k + 1] = wgsl_i32((Y[k] * rs1) * 65536.0f);
+                val[6 + 3 * k + 2] = wgsl_i32((Y[k] * rs2) * 65536.0f);
+              }
+            }
+            float fg = r0 * cr + r1 * cg;
+            fg = fg + r2 * cbl;
+            float bgt = r0 * acc0 + r1 * acc1;
+            bgt = bgt + r2 * acc2;
+            const float dLda = (fg - bgt) * Tb;
+            const float dlogit = (dLda * a) * (1.0f - op);
+            const float dLdG = dLda * op;
+            const float dLds = dLdG * (-G);
+            val[0] = wgsl_i32(dlogit * 65536.0f);
+            val[1] = wgsl_i32((((dLds * 0.5f) * dx) * dx) * 65536.0f);
+            val[2] = wgsl_i32(((dLds * dx) * dy) * 65536.0f);
+            val[3] = wgsl_i32((((dLds * 0.5f) * dy) * dy) * 65536.0f);
+            val[4] = wgsl_i32((-(dLds * ((q0.z * dx) + (q0.w * dy)))) * 65536.0f);
+            val[5] = wgsl_i32((-(dLds * ((q0.w * dx) + (q1.x * dy)))) * 65536.0f);
+            acc0 = a * cr + (1.0f - a) * acc0;
+            acc1 = a * cg + (1.0f - a) * acc1;
+            acc2 = a * cbl + (1.0f - a) * acc2;
+            T = Tb;
+          }
+        }
+      }
+      if (__any_sync(kFull, contrib)) {
+#pragma unroll
+        for (int k = 0; k < 54; ++k) {
+          int s = val[k];
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1)
+            s = (int)((uint32_t)s + (uint32_t)__shfl_xor_sync(kFull, s, o));
+          val[k] = s;
+        }
+        // lane k adds slot k and k + 32 (integer, order-independent)
+#pragma unroll
+        for (int k = 0; k < 54; ++k)
+          if ((k & 31) == (int)lane && val[k] != 0) atomicAdd(&s_tg[jj][k], val[k]);
+      }
+    }
+    __syncthreads();
+    for (int k = tid; k < cnt * 54; k += NT) {
+      const int jj = k / 54, slot = k % 54;
+      const int s = s_tg[jj][slot];
+      const uint32_t i = bs + (uint32_t)jj;
+      b.tile_grads[(size_t)i * 54 + slot] = s;
+      if (s != 0) atomicAdd((unsigned long long*)&b.gsum54[(size_t)b.flatten[i] * 54 + slot],
+                            (unsigned long long)(long long)s);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Geometry adjoint + SH chain + Adam, one thread per Gaussian.  For each view
+// of the step: sum the Gaussian's per-intersection partials (contiguous in
+// emission order, summed in order), then back-propagate dL/d(colour, logit,
+// conic, mean2d) through the projection as implemented (training-tiles.wgsl:
+// 126-223) to position, log sigma, quaternion, opacity logit and SH.  The
+// per-view gradients are added in view order.  Then adam.wgsl:18-38 per
+// plane with the group's learning rate.
+// ---------------------------------------------------------------------------
+struct Grad11 {
+  float pos[3], ls[3], q[4], logit;
+};
+
+SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& sp,
+                        const float* prm /*11 geometry params*/, const float in9[9],
+                        bool color_dir, const float* sh /*48, may be null*/, int deg,
+                        Grad11& gr) {
+  // mean -> camera space
+  float dpc[3] = {0.f, 0.f, 0.f};
+  float clip[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) clip[r] = mat4_row(vi.proj, r, o.pc[0], o.pc[1], o.pc[2], o.pc[3]);
+  const float ndx = clip[0] / clip[3], ndy = clip[1] / clip[3];
+  const float hW = 0.5f * (float)vi.width, hH = 0.5f * (float)vi.height;
+#pragma unroll
+  for (int j = 0; j < 3; ++j) {
+    dpc[j] += in9[7] * hW * (vi.proj[j * 4 + 0] - ndx * vi.proj[j * 4 + 3]) / clip[3];
+    dpc[j] += in9[8] * hH * (vi.proj[j * 4 + 1] - ndy * vi.proj[j * 4 + 3]) / clip[3];
+  }
+  // covariance
+  float sig[3], lsg[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float raw = prm[3 + k];
+    sig[k] = expf(clampf_(raw, -10.0f, 10.0f));
+    lsg[k] = (raw > -10.0f && raw < 10.0f) ? 1.0f : 0.0f;
+  }
+  const float qr0 = prm[6], qr1 = prm[7], qr2 = prm[8], qr3 = prm[9];
+  const float ql = sqrtf(qr0 * qr0 + qr1 * qr1 + qr2 * qr2 + qr3 * qr3);
+  const float x = qr0 / ql, y = qr1 / ql, z = qr2 / ql, w = qr3 / ql;
+  float R[3][3] = {{1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y)},
+                   {2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x)},
+                   {2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y)}};
+  float M[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) M[a][c] = R[a][c] * sig[c];
+  float C3[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) C3[a][c] = M[a][0] * M[c][0] + M[a][1] * M[c][1] + M[a][2] * M[c][2];
+  float V3[3][3];  // math rows
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) V3[r][j] = vi.view[j * 4 + r];
+  float tmp[3][3], Wm[2][2];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) tmp[a][c] = V3[a][0] * C3[0][c] + V3[a][1] * C3[1][c] + V3[a][2] * C3[2][c];
+#pragma unroll
+  for (int a = 0; a < 2; ++a)
+#pragma unroll
+    for (int c = 0; c < 2; ++c) Wm[a][c] = tmp[a][0] * V3[c][0] + tmp[a][1] * V3[c][1] + tmp[a][2] * V3[c][2];
+  const float tz = o.pc[2];
+  const float kx = vi.focal[0] / tz, ky = vi.focal[1] / tz;
+  const float C00 = kx * kx * Wm[0][0], C01 = kx * ky * Wm[0][1], C11 = ky * ky * Wm[1][1];
+  const float e00 = C00 + sp.eps2d, e11 = C11 + sp.eps2d;
+  const float det = e00 * e11 - C01 * C01;
+  const float Qa = e11 / det, Qb = -C01 / det, Qc = e00 / det;
+  const float ga = in9[4], gb = 0.5f * in9[5], gc = in9[6];
+  // dC = -Q GQ Q (2x2 symmetric)
+  const float t00 = ga * Qa + gb * Qb, t01 = ga * Qb + gb * Qc;
+  const float t10 = gb * Qa + gc * Qb, t11 = gb * Qb + gc * Qc;
+  const float dC00 = -(Qa * t00 + Qb * t10);
+  const float dC01a = -(Qa * t01 + Qb * t11);
+  const float dC10a = -(Qb * t00 + Qc * t10);
+  const float dC11 = -(Qb * t01 + Qc * t11);
+  const float dC01 = dC01a + dC10a;
+  const float dW00 = dC00 * kx * kx, dW01 = dC01 * kx * ky, dW11 = dC11 * ky * ky;
+  dpc[2] += -2.0f / tz * (dC00 * C00 + dC01 * C01 + dC11 * C11);
+  // G3 = V3^T GW V3 with GW = [[dW00, dW01/2, 0], [dW01/2, dW11, 0], [0, 0, 0]]
+  float G3[3][3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      G3[a][c] = V3[0][a] * (dW00 * V3[0][c] + 0.5f * dW01 * V3[1][c]) +
+                 V3[1][a] * (0.5f * dW01 * V3[0][c] + dW11 * V3[1][c]);
+  float dR[3][3], dsig[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const float dM = 2.0f * (G3[a][0] * M[0][c] + G3[a][1] * M[1][c] + G3[a][2] * M[2][c]);
+      dR[a][c] = dM * sig[c];
+      dsig[c] += dM * R[a][c];
+    }
+  float dq[4];
+  dq[0] = 2 * y * (dR[0][1] + dR[1][0]) + 2 * z * (dR[0][2] + dR[2][0]) +
+          2 * w * (dR[2][1] - dR[1][2]) - 4 * x * (dR[1][1] + dR[2][2]);
+  dq[1] = -4 * y * (dR[0][0] + dR[2][2]) + 2 * x * (dR[0][1] + dR[1][0]) +
+          2 * w * (dR[0][2] - dR[2][0]) + 2 * z * (dR[1][2] + dR[2][1]);
+  dq[2] = -4 * z * (dR[0][0] + dR[1][1]) + 2 * w * (dR[1][0] - dR[0][1]) +
+          2 * x * (dR[0][2] + dR[2][0]) + 2 * y * (dR[1][2] + dR[2][1]);
+  dq[3] = -2 * z * dR[0][1] + 2 * y * dR[0][2] + 2 * z * dR[1][0] - 2 * x * dR[1][2] -
+          2 * y * dR[2][0] + 2 * x * dR[2][1];
+  const float qd = x * dq[0] + y * dq[1] + z * dq[2] + w * dq[3];
+  const float qn[4] = {x, y, z, w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) gr.q[k] += (dq[k] - qn[k] * qd) / ql;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gr.ls[k] += dsig[k] * sig[k] * lsg[k];
+  gr.logit += in9[3];
+  // colour -> view direction
+  if (color_dir && deg > 0 && sh) {
+    const float X = o.dir[0], Yv = o.dir[1], Z = o.dir[2];
+    float draw[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) draw[c] = o.raw[c] > 0.0f ? in9[c] : 0.0f;
+    float ddir[3] = {0.f, 0.f, 0.f};
+    auto addk = [&](int k, float gx, float gy, float gz) {
+      float s = draw[0] * sh[3 * k] + draw[1] * sh[3 * k + 1] + draw[2] * sh[3 * k + 2];
+      ddir[0] += s * gx;
+      ddir[1] += s * gy;
+      ddir[2] += s * gz;
+    };
+    addk(1, 0.f, -SH_C1, 0.f);
+    addk(2, 0.f, 0.f, SH_C1);
+    addk(3, -SH_C1, 0.f, 0.f);
+    if (deg > 1) {
+      addk(4, SH_C2_0 * Yv, SH_C2_0 * X, 0.f);
+      addk(5, 0.f, SH_C2_1 * Z, SH_C2_1 * Yv);
+      addk(6, -2.f * SH_C2_2 * X, -2.f * SH_C2_2 * Yv, 4.f * SH_C2_2 * Z);
+      addk(7, SH_C2_3 * Z, 0.f, SH_C2_3 * X);
+      addk(8, 2.f * SH_C2_4 * X, -2.f * SH_C2_4 * Yv, 0.f);
+    }
+    if (deg > 2) {
+      const float xx = X * X, yy = Yv * Yv, zz = Z * Z;
+      addk(9, SH_C3_0 * 6.f * X * Yv, SH_C3_0 * (3.f * xx - 3.f * yy), 0.f);
+      addk(10, SH_C3_1 * Yv * Z, SH_C3_1 * X * Z, SH_C3_1 * X * Yv);
+      addk(11, SH_C3_2 * (-2.f * X * Yv), SH_C3_2 * (4.f * zz - xx - 3.f * yy), SH_C3_2 * 8.f * Yv * Z);
+      addk(12, SH_C3_3 * (-6.f * X * Z), SH_C3_3 * (-6.f * Yv * Z), SH_C3_3 * (6.f * zz - 3.f * xx - 3.f * yy));
+      addk(13, SH_C3_4 * (4.f * zz - 3.f * xx - yy), SH_C3_4 * (-2.f * X * Yv), SH_C3_4 * 8.f * X * Z);
+      addk(14, SH_C3_5 * 2.f * X * Z, SH_C3_5 * (-2.f * Yv * Z), SH_C3_5 * (xx - yy));
+      addk(15, SH_C3_6 * (3.f * xx - 3.f * yy), SH_C3_6 * (-6.f * X * Yv), 0.f);
+    }
+    float vl = sqrtf(o.pc[0] * o.pc[0] + o.pc[1] * o.pc[1] + o.pc[2] * o.pc[2]);
+    const float dd = X * ddir[0] + Yv * ddir[1] + Z * ddir[2];
+    dpc[0] += -(ddir[0] - X * dd) / vl;
+    dpc[1] += -(ddir[1] - Yv * dd) / vl;
+    dpc[2] += -(ddir[2] - Z * dd) / vl;
+  }
+#pragma unroll
+  for (int j = 0; j < 3; ++j) gr.pos[j] += V3[0][j] * dpc[0] + V3[1][j] * dpc[1] + V3[2][j] * dpc[2];
+}
+
+SKY_DEV void adam_elem(float* __restrict__ p, float* __restrict__ m1, float* __restrict__ m2,
+                       size_t idx, float g, float lr, const StepParams& sp) {
+  const float pm1 = m1[idx], pm2 = m2[idx];
+  const float a = sp.beta1 * pm1;
+  const float bb = (1.0f - sp.beta1) * g;
+  const float nm1 = a + bb;
+  const float c = sp.beta2 * pm2;
+  const float d = ((1.0f - sp.beta2) * g) * g;
+  const float nm2 = c + d;
+  const float denom = sqrtf(nm2) * sp.bc2_sqrt_rcp + sp.adam_eps;
+  const float step = lr * sp.bc1_rcp;
+  p[idx] = p[idx] - step * (nm1 / denom);
+  m1[idx] = nm1;
+  m2[idx] = nm2;
+}
+
+__global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  if (capacity_failed(b.status)) return;
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= sp.n) return;
+  const uint32_t stride = sp.plane_stride;
+  const bool r16 = sp.round_f16 != 0;
+  const int deg = (int)sp.sh_deg;
+  const int ncoef = (deg + 1) * (deg + 1);
+  const bool ref = sp.bwd_mode != 0;
+  const bool need_sh_grads = sp.sh_update || sp.write_grads;
+  float prm[11];
+#pragma unroll
+  for (int k = 0; k < 11; ++k) prm[k] = load_plane_rw(b.params, stride, k, g, r16);
+  float sh[48];
+#pragma unroll
+  for (int k = 0; k < 48; ++k)
+    sh[k] = (!ref && k < 3 * ncoef) ? load_plane_rw(b.params, stride, 11 + k, g, r16) : 0.0f;
+  Grad11 gr;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) { gr.pos[k] = 0.f; gr.ls[k] = 0.f; }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) gr.q[k] = 0.f;
+  gr.logit = 0.f;
+  float gsh[48];
+#pragma unroll
+  for (int k = 0; k < 48; ++k) gsh[k] = 0.0f;
+  auto get = [&](int plane) {
+    return plane < 11 ? prm[plane] : (plane - 11 < 48 ? sh[plane - 11] : 0.0f);
+  };
+  for (uint32_t v = 0; v < sp.num_views; ++v) {
+    const size_t item = (size_t)v * sp.n + g;
+    const uint32_t cnt = b.counts[item];
+    if (cnt == 0) continue;
+    float in9[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
+    float shref[48];
+    if (!ref) {
+      const uint32_t e1 = b.cumsum[item], e0 = e1 - cnt;
+      for (uint32_t e = e0; e < e1; ++e) {
+        const float4 a0 = b.partials[(size_t)e * 3 + 0];
+        const float4 a1 = b.partials[(size_t)e * 3 + 1];
+        const float4 a2 = b.partials[(size_t)e * 3 + 2];
+        in9[0] = in9[0] + a0.x; in9[1] = in9[1] + a0.y; in9[2] = in9[2] + a0.z;
+        in9[3] = in9[3] + a0.w; in9[4] = in9[4] + a1.x; in9[5] = in9[5] + a1.y;
+        in9[6] = in9[6] + a1.z; in9[7] = in9[7] + a1.w; in9[8] = in9[8] + a2.x;
+      }
+    } else {
+      const long long* s = b.gsum54 + item * 54;
+      const float sc = 1.0f / 65536.0f;
+      in9[3] = (float)s[0] * sc;
+      in9[4] = (float)s[1] * sc; in9[5] = (float)s[2] * sc; in9[6] = (float)s[3] * sc;
+      in9[7] = (float)s[4] * sc; in9[8] = (float)s[5] * sc;
+#pragma unroll
+      for (int k = 0; k < 48; ++k) shref[k] = (float)s[6 + k] * sc;
+    }
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < 9; ++k) any = any || in9[k] != 0.0f;
+    if (ref) {
+#pragma unroll
+      for (int k = 0; k < 48; ++k) any = any || shref[k] != 0.0f;
+    }
+    if (!any) continue;
+    const ViewInfo& vi = sp.views[v];
+    ProjOut o;
+    if (!project_gaussian(get, vi, sp, deg, !ref, o)) continue;
+    geom_chain(o, vi, sp, prm, in9, !ref, sh, deg, gr);
+    if (need_sh_grads) {
+      if (!ref) {
+        float Y[16];
+        sh_basis(o.dir[0], o.dir[1], o.dir[2], deg, Y);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float dr = o.raw[c] > 0.0f ? in9[c] : 0.0f;
+#pragma unroll
+          for (int k = 0; k < 16; ++k)
+            if (k < ncoef) gsh[3 * k + c] += Y[k] * dr;
+        }
+      } else {
+#pragma unroll
+        for (int k = 0; k < 48; ++k) gsh[k] += shref[k];
+      }
+    }
+  }
+  float g11[11] = {gr.pos[0], gr.pos[1], gr.pos[2], gr.ls[0], gr.ls[1], gr.ls[2],
+                   gr.q[0],   gr.q[1],   gr.q[2],   gr.q[3],  gr.logit};
+  if (sp.write_grads) {
+#pragma unroll
+    for (int k = 0; k < 11; ++k) b.grads[(size_t)k * stride + g] = g11[k];
+#pragma unroll
+    for (int k = 0; k < 48; ++k) b.grads[(size_t)(11 + k) * stride + g] = gsh[k];
+  }
+  if (sp.apply_adam) {
+#pragma unroll
+    for (int k = 0; k < 11; ++k) {
+      const float lr = k < 3 ? sp.lr_pos : (k < 6 ? sp.lr_scale : (k < 10 ? sp.lr_rot : sp.lr_opacity));
+      adam_elem(b.params, b.m1, b.m2, (size_t)k * stride + g, g11[k], lr, sp);
+    }
+    if (sp.sh_update) {
+#pragma unroll
+      for (int k = 0; k < 48; ++k)
+        adam_elem(b.params, b.m1, b.m2, (size_t)(11 + k) * stride + g, gsh[k], sp.lr_sh, sp);
+    }
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Launchers
+// ---------------------------------------------------------------------------
+void launch_preprocess(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s) {
+  dim3 grid((n + 255) / 256, views);
+  k_preprocess<<<grid, 256, 0, s>>>(b);
+}
+
+void launch_scan(const DevBuffers& b, uint32_t n_items, cudaStream_t s) {
+  const uint32_t nb = (n_items + kScanTile - 1) / kScanTile;
+  if (nb == 0) return;
+  k_scan_reduce<<<nb, kScanThreads, 0, s>>>(b, n_items);
+  k_scan_blocks<<<1, 1024, 0, s>>>(b, nb);
+  k_scan_final<<<nb, kScanThreads, 0, s>>>(b, n_items);
+}
+
+uint32_t scan_block_count(uint32_t n_items) { return (n_items + kScanTile - 1) / kScanTile; }
+
+void launch_group_bounds(const DevBuffers& b, cudaStream_t s) { k_group_bounds<<<1, 64, 0, s>>>(b); }
+
+void launch_emit(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s) {
+  dim3 grid((n + 255) / 256, views);
+  k_emit<<<grid, 256, 0, s>>>(b);
+}
+
+void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s) {
+  if (icap) k_ranges<<<(icap + 255) / 256, 256, 0, s>>>(b);
+  k_ranges_empty<<<1, 256, 0, s>>>(b);
+}
+
+void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ssim,
+                    uint32_t views, uint32_t max_view_pixels, cudaStream_t s) {
+  if (max_tiles == 0) return;
+  switch (ts) {
+    case 8: k_forward<8><<<max_tiles, 64, 0, s>>>(b); break;
+    case 32: k_forward<32><<<max_tiles, 1024, 0, s>>>(b); break;
+    default: k_forward<16><<<max_tiles, 256, 0, s>>>(b); break;
+  }
+  if (ssim) {
+    dim3 grid((max_view_pixels + 255) / 256, views);
+    k_ssim<<<grid, 256, 0, s>>>(b);
+  }
+}
+
+void launch_loss_final(const DevBuffers& b, cudaStream_t s) { k_loss_final<<<1, 1024, 0, s>>>(b); }
+
+void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ref, cudaStream_t s) {
+  if (max_tiles == 0) return;
+  if (!ref) {
+    switch (ts) {
+      case 8: k_backward_exact<8><<<max_tiles, 64, 0, s>>>(b); break;
+      case 32: k_backward_exact<32><<<max_tiles, 1024, 0, s>>>(b); break;
+      default: k_backward_exact<16><<<max_tiles, 256, 0, s>>>(b); break;
+    }
+  } else {
+    switch (ts) {
+      case 8: k_backward_ref<8><<<max_tiles, 64, 0, s>>>(b); break;
+      case 32: k_backward_ref<32><<<max_tiles, 1024, 0, s>>>(b); break;
+      default: k_backward_ref<16><<<max_tiles, 256, 0, s>>>(b); break;
+    }
+  }
+}
+
+void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s) {
+  if (n == 0) return;
+  k_geom_adam<<<(n + 127) / 128, 128, 0, s>>>(b);
+}
+
+}  // namespace sky

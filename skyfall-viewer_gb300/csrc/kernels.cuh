@@ -1,0 +1,30 @@
+// Launch interface of the hot-path kernels (kernels.cu).
+#pragma once
+
+#include "sky_types.cuh"
+#include "sort.cuh"
+
+namespace sky {
+
+void launch_preprocess(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s);
+void launch_scan(const DevBuffers& b, uint32_t n_items, cudaStream_t s);
+uint32_t scan_block_count(uint32_t n_items);
+void launch_group_bounds(const DevBuffers& b, cudaStream_t s);
+void launch_emit(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s);
+void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s);
+void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ssim,
+                    uint32_t views, uint32_t max_view_pixels, cudaStream_t s);
+void launch_loss_final(const DevBuffers& b, cudaStream_t s);
+void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ref,
+                     cudaStream_t s);
+void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s);
+
+// Prune / densify / opacity reset (compact.cu).
+void launch_prune_flags(const float* params, uint32_t stride, uint32_t n, float min_opacity,
+                        float max_scale, const uint8_t* mask, uint32_t* flags, cudaStream_t s);
+void launch_compact(const float* src, float* dst, uint32_t src_stride, uint32_t dst_stride,
+                    uint32_t planes, uint32_t n, const uint32_t* keep_scan, cudaStream_t s);
+void launch_reset_opacity(float* params, uint32_t stride, uint32_t n, float max_logit,
+                          cudaStream_t s);
+
+}  // namespace sky

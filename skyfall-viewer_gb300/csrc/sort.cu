@@ -1,0 +1,283 @@
+// Onesweep LSD radix sort (see sort.cuh).
+#include "sort.cuh"
+
+namespace sky {
+namespace {
+
+constexpr uint32_t kFlagAgg = 1u << 30;
+constexpr uint32_t kFlagPrefix = 2u << 30;
+constexpr uint32_t kValueMask = (1u << 30) - 1u;
+constexpr uint32_t kSpinLimit = 1u << 20;
+constexpr int kWarps = kSortThreads / 32;
+
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+  asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ uint32_t lanemask_lt() {
+  uint32_t m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+__device__ __forceinline__ void seg_bounds(const SortSegment& s, uint32_t& b, uint32_t& n) {
+  if (s.bounds) {
+    b = s.bounds[0];
+    uint32_t e = s.bounds[1];
+    n = e > b ? e - b : 0u;
+  } else {
+    b = 0;
+    n = s.n;
+  }
+}
+
+// Digit counts of every pass in one read of the keys; also clears the
+// look-back words of the tiles this segment will use.
+__global__ void __launch_bounds__(kSortThreads)
+k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes,
+            uint32_t* __restrict__ hist, uint32_t* __restrict__ lookback, uint32_t max_tiles) {
+  __shared__ uint32_t s_hist[kMaxPasses][kRadix];
+  for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kSortThreads) (&s_hist[0][0])[i] = 0;
+  uint32_t begin, n;
+  seg_bounds(seg, begin, n);
+  // clear look-back words of this segment's tiles
+  uint32_t tiles = (n + kSortTile - 1) / kSortTile;
+  uint64_t words = (uint64_t)tiles * kRadix;
+  for (int p = 0; p < passes; ++p)
+    for (uint64_t w = (uint64_t)blockIdx.x * kSortThreads + threadIdx.x; w < words;
+         w += (uint64_t)gridDim.x * kSortThreads)
+      lookback[(uint64_t)p * max_tiles * kRadix + w] = 0u;
+  __syncthreads();
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t warp_global = (blockIdx.x * kSortThreads + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * kSortThreads) >> 5;
+  // warp-strided chunks of 32 consecutive keys
+  for (uint32_t base = warp_global * 32; base < n; base += nwarps * 32) {
+    uint32_t idx = base + lane;
+    bool valid = idx < n;
+    uint32_t k = valid ? keys[begin + idx] : 0u;
+    uint32_t active = __ballot_sync(0xFFFFFFFFu, valid);
+    if (valid) {
+      for (int p = 0; p < passes; ++p) {
+        uint32_t d = (k >> (8 * p)) & 0xFFu;
+        uint32_t peers = __match_any_sync(active, d);
+        if ((peers & lanemask_lt()) == 0) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < passes * kRadix; i += kSortThreads) {
+    uint32_t v = (&s_hist[0][0])[i];
+    if (v) atomicAdd(&hist[i], v);
+  }
+}
+
+// Exclusive scan of each pass's 256 digit counts (one block per pass).
+__global__ void __launch_bounds__(kRadix) k_sort_scan(uint32_t* __restrict__ hist) {
+  __shared__ uint32_t s_warp[kRadix / 32];
+  uint32_t* h = hist + blockIdx.x * kRadix;
+  uint32_t v = h[threadIdx.x];
+  uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) s_warp[warp] = x;
+  __syncthreads();
+  uint32_t add = 0;
+  for (uint32_t w = 0; w < warp; ++w) add += s_warp[w];
+  h[threadIdx.x] = x - v + add;
+}
+
+__global__ void __launch_bounds__(kSortThreads)
+k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+           uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, SortSegment seg,
+           int pass, const uint32_t* __restrict__ hist, uint32_t* __restrict__ tile_counter,
+           uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err) {
+  __shared__ uint32_t s_keys[kSortTile];
+  __shared__ uint32_t s_vals[kSortTile];
+  __shared__ uint32_t s_warp_hist[kWarps][kRadix];
+  __shared__ uint32_t s_block_excl[kRadix];
+  __shared__ uint32_t s_global[kRadix];
+  __shared__ uint32_t s_scan[kWarps];
+  __shared__ uint32_t s_tile;
+
+  uint32_t begin, n;
+  seg_bounds(seg, begin, n);
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(&tile_counter[pass], 1u);
+  for (int i = tid; i < kWarps * kRadix; i += kSortThreads) (&s_warp_hist[0][0])[i] = 0u;
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t base = tile * (uint32_t)kSortTile;
+  if (base >= n) return;
+  const int shift = 8 * pass;
+
+  uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
+  const uint32_t lt = lanemask_lt();
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    uint32_t idx = base + warp * (32 * kSortItems) + k * 32 + lane;
+    bool valid = idx < n;
+    key[k] = valid ? keys_in[begin + idx] : 0xFFFFFFFFu;
+    val[k] = valid ? (vals_in ? vals_in[begin + idx] : begin + idx) : 0u;
+  }
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    uint32_t idx = base + warp * (32 * kSortItems) + k * 32 + lane;
+    bool valid = idx < n;
+    uint32_t d = (key[k] >> shift) & 0xFFu;
+    uint32_t active = __ballot_sync(0xFFFFFFFFu, valid);
+    uint32_t peers = 0, cnt = 0;
+    if (valid) {
+      peers = __match_any_sync(active, d);
+      cnt = s_warp_hist[warp][d];
+    }
+    __syncwarp();
+    if (valid && (peers & lt) == 0) s_warp_hist[warp][d] = cnt + __popc(peers);
+    __syncwarp();
+    rank[k] = valid ? cnt + __popc(peers & lt) : 0xFFFFFFFFu;
+  }
+  __syncthreads();
+
+  // Per digit (thread = digit): per-warp exclusive prefix and tile count.
+  const uint32_t d = tid;
+  uint32_t run = 0;
+#pragma unroll
+  for (int w = 0; w < kWarps; ++w) {
+    uint32_t c = s_warp_hist[w][d];
+    s_warp_hist[w][d] = run;
+    run += c;
+  }
+  uint32_t* lb = lookback + ((uint64_t)pass * max_tiles) * kRadix;
+  st_relaxed(&lb[(uint64_t)tile * kRadix + d], (tile == 0 ? kFlagPrefix : kFlagAgg) | run);
+
+  // Exclusive scan of tile counts over digits.
+  uint32_t x = run;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+    if (lane >= (uint32_t)o) x += y;
+  }
+  if (lane == 31) s_scan[warp] = x;
+
+  // Decoupled look-back for this digit.
+  uint32_t excl = 0;
+  if (tile > 0) {
+    int64_t j = (int64_t)tile - 1;
+    uint32_t spins = 0;
+    while (j >= 0) {
+      uint32_t v = ld_relaxed(&lb[(uint64_t)j * kRadix + d]);
+      uint32_t flag = v & ~kValueMask;
+      if (flag == 0u) {
+        if (++spins > kSpinLimit) {
+          atomicOr(err, SKY_DEVERR_SORT_TIMEOUT);
+          break;
+        }
+        if (spins > 16) __nanosleep(64);
+        continue;
+      }
+      excl += v & kValueMask;
+      if (flag == kFlagPrefix) break;
+      --j;
+    }
+    st_relaxed(&lb[(uint64_t)tile * kRadix + d], kFlagPrefix | (excl + run));
+  }
+  __syncthreads();
+  uint32_t add = 0;
+  for (uint32_t w = 0; w < warp; ++w) add += s_scan[w];
+  const uint32_t bex = x - run + add;
+  s_block_excl[d] = bex;
+  s_global[d] = hist[pass * kRadix + d] + excl;
+  __syncthreads();
+
+  // Local scatter (stable) into shared memory.
+#pragma unroll
+  for (int k = 0; k < kSortItems; ++k) {
+    if (rank[k] != 0xFFFFFFFFu) {
+      uint32_t dk = (key[k] >> shift) & 0xFFu;
+      uint32_t lp = s_block_excl[dk] + s_warp_hist[warp][dk] + rank[k];
+      s_keys[lp] = key[k];
+      s_vals[lp] = val[k];
+    }
+  }
+  __syncthreads();
+  const uint32_t cnt = min((uint32_t)kSortTile, n - base);
+  for (uint32_t i = tid; i < cnt; i += kSortThreads) {
+    uint32_t kk = s_keys[i];
+    uint32_t dk = (kk >> shift) & 0xFFu;
+    uint32_t gp = s_global[dk] + (i - s_block_excl[dk]);
+    keys_out[begin + gp] = kk;
+    vals_out[begin + gp] = s_vals[i];
+  }
+}
+
+}  // namespace
+
+size_t sort_scratch_bytes(uint32_t max_n) {
+  uint32_t tiles = (max_n + kSortTile - 1) / kSortTile + 1;
+  size_t b = 0;
+  b += kMaxPasses * kRadix * 4;                    // hist
+  b += 256;                                        // tile counters (padded)
+  b += (size_t)kMaxPasses * tiles * kRadix * 4;    // look-back
+  b += (size_t)(max_n + 64) * 4 * 2;               // ping-pong
+  return b + 1024;
+}
+
+SortScratch sort_scratch_carve(void* base, uint32_t max_n) {
+  uint32_t tiles = (max_n + kSortTile - 1) / kSortTile + 1;
+  char* p = (char*)base;
+  auto take = [&](size_t bytes) {
+    char* r = p;
+    p += (bytes + 255) & ~(size_t)255;
+    return r;
+  };
+  SortScratch s;
+  s.hist = (uint32_t*)take(kMaxPasses * kRadix * 4);
+  s.tile_counter = (uint32_t*)take(256);
+  s.lookback = (uint32_t*)take((size_t)kMaxPasses * tiles * kRadix * 4);
+  s.keys_tmp = (uint32_t*)take((size_t)(max_n + 64) * 4);
+  s.vals_tmp = (uint32_t*)take((size_t)(max_n + 64) * 4);
+  s.max_tiles = tiles;
+  return s;
+}
+
+cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
+                              uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
+                              uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
+                              uint32_t* err, cudaStream_t stream) {
+  if (key_bits == 0) key_bits = 1;
+  if (key_bits > 32) key_bits = 32;
+  const int passes = (int)((key_bits + 7) / 8);
+  cudaError_t e = cudaMemsetAsync(sc.hist, 0, kMaxPasses * kRadix * 4, stream);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(sc.tile_counter, 0, 256, stream);
+  if (e != cudaSuccess) return e;
+  uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
+  if (tiles == 0) tiles = 1;
+  uint32_t hist_blocks = tiles < 1024u ? tiles : 1024u;
+  k_sort_hist<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, seg, passes, sc.hist,
+                                                         sc.lookback, sc.max_tiles);
+  k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist);
+  const uint32_t* src_k = keys_in;
+  const uint32_t* src_v = vals_in;
+  for (int p = 0; p < passes; ++p) {
+    bool to_out = ((passes - 1 - p) % 2) == 0;
+    uint32_t* dk = to_out ? keys_out : sc.keys_tmp;
+    uint32_t* dv = to_out ? vals_out : sc.vals_tmp;
+    k_onesweep<<<tiles, kSortThreads, 0, stream>>>(src_k, src_v, dk, dv, seg, p, sc.hist,
+                                                    sc.tile_counter, sc.lookback, sc.max_tiles,
+                                                    err);
+    src_k = dk;
+    src_v = dv;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace sky

@@ -1,0 +1,259 @@
+"""Host-side mirror of the reference's GaussianRenderer training API.
+
+Method names, argument meaning and defaults follow the object returned by
+get_renderer (src/renderers/gaussian-renderer.ts:30-58, 4110-4153); each call
+goes straight to the C-ABI (include/skyfall.h).  Differences that follow from
+the host: calls are synchronous (the reference returns Promises), images are
+numpy arrays (the reference binds GPU textures), and camera choice in
+train() comes from a seeded generator instead of Math.random().
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+
+@dataclass
+class TrainingParams:
+    """TrainingParams (gaussian-renderer.ts:100-107)."""
+    lr_means: float
+    lr_sh: float
+    lr_opacity: float
+    lr_scale: float
+    lr_rotation: float
+    sh_update_interval: int
+
+
+@dataclass
+class LossWeights:
+    """LossWeights (gaussian-renderer.ts:110-114)."""
+    w_l2: float
+    w_l1: float
+    w_ssim: float
+
+
+@dataclass
+class TrainingStatus:
+    """TrainingStatus (gaussian-renderer.ts:117-123)."""
+    isTraining: bool
+    currentIteration: int
+    targetIterations: int
+    iterationsPerSecond: float
+    gaussianCount: int
+
+
+def to_sky_camera(cam) -> L.SkyCamera:
+    if isinstance(cam, L.SkyCamera):
+        return cam
+    c = L.SkyCamera()
+    c.view = (C.c_float * 16)(*np.asarray(cam["view"], dtype=np.float32).reshape(16))
+    c.proj = (C.c_float * 16)(*np.asarray(cam["proj"], dtype=np.float32).reshape(16))
+    c.focal = (C.c_float * 2)(*np.asarray(cam["focal"], dtype=np.float32).reshape(2))
+    c.width = int(cam["width"])
+    c.height = int(cam["height"])
+    return c
+
+
+class GaussianRenderer:
+    """A skyfall context: one scene, its cameras and targets, its optimizer."""
+
+    def __init__(self, config: L.SkyConfig | None = None, **overrides):
+        self._L = L.lib()
+        self.config = config if config is not None else L.default_config(**overrides)
+        h = C.c_void_p()
+        L.check(self._L.sky_create(C.byref(self.config), C.byref(h)))
+        self._h = h
+        self._cams: list[L.SkyCamera] = []
+        self._stop = False
+        self._training = False
+        self._target_iters = 0
+        self._ips = 0.0
+        self.last_stats = L.SkyStepStats()
+
+    # -- lifecycle ----------------------------------------------------------
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self._L.sky_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # -- scene --------------------------------------------------------------
+    def load_points(self, params: np.ndarray) -> None:
+        """params: (59, N) f32 planes (see SKY_PLANE_*)."""
+        p = np.ascontiguousarray(params, dtype=np.float32)
+        if p.ndim != 2 or p.shape[0] != L.SKY_NUM_PLANES:
+            raise ValueError("params must be (59, N)")
+        L.check(self._L.sky_load_points(self._h, L.ptr(p), p.shape[1], p.shape[1]))
+
+    def load_packed(self, gaussians: np.ndarray, sh: np.ndarray | None) -> None:
+        """Reference storage: gaussians (N, 6) u32 words, sh (N, 24) u32 words."""
+        g = np.ascontiguousarray(gaussians, dtype=np.uint32)
+        s = None if sh is None else np.ascontiguousarray(sh, dtype=np.uint32)
+        L.check(self._L.sky_load_packed(self._h, L.ptr(g), L.ptr(s), g.shape[0]))
+
+    def setTrainingCameras(self, cameras) -> None:
+        self._cams = [to_sky_camera(c) for c in cameras]
+        arr = (L.SkyCamera * len(self._cams))(*self._cams)
+        L.check(self._L.sky_set_cameras(self._h, arr, len(self._cams)))
+
+    def setTrainingImages(self, images) -> None:
+        for i, img in enumerate(images):
+            self.setTrainingImage(i, img)
+
+    def setTrainingImage(self, camera: int, image: np.ndarray) -> None:
+        a = np.ascontiguousarray(image, dtype=np.float32)
+        if a.ndim != 3 or a.shape[2] < 3:
+            raise ValueError("image must be (H, W, 3)")
+        a = np.ascontiguousarray(a[:, :, :3])
+        L.check(self._L.sky_set_target(self._h, camera, L.ptr(a), a.shape[1], a.shape[0]))
+
+    # -- hot path -----------------------------------------------------------
+    def buildTrainingTiles(self, camera: int = 0) -> None:
+        """Project, emit, sort and range the tiles of one camera (the forward
+        of that camera also runs; the tile buffers stay readable)."""
+        self.render([camera])
+
+    def render(self, cameras, with_alpha: bool = True):
+        cams = np.ascontiguousarray(np.atleast_1d(cameras), dtype=np.uint32)
+        px = sum(self._cams[int(c)].width * self._cams[int(c)].height for c in cams)
+        rgba = np.empty((px, 4), dtype=np.float32)
+        alpha = np.empty(px, dtype=np.float32) if with_alpha else None
+        L.check(self._L.sky_render(self._h, L.ptr(cams), len(cams), L.ptr(rgba), L.ptr(alpha)))
+        return rgba, alpha
+
+    def forward(self, cameras) -> float:
+        cams = np.ascontiguousarray(np.atleast_1d(cameras), dtype=np.uint32)
+        loss = C.c_double()
+        L.check(self._L.sky_forward(self._h, L.ptr(cams), len(cams), C.byref(loss)))
+        return loss.value
+
+    def backward(self) -> np.ndarray:
+        n = self.getGaussianCount()
+        g = np.empty((L.SKY_NUM_PLANES, n), dtype=np.float32)
+        L.check(self._L.sky_backward(self._h, L.ptr(g), n))
+        return g
+
+    def trainStep(self, cameras) -> L.SkyStepStats:
+        cams = np.ascontiguousarray(np.atleast_1d(cameras), dtype=np.uint32)
+        st = L.SkyStepStats()
+        L.check(self._L.sky_step(self._h, L.ptr(cams), len(cams), C.byref(st)))
+        self.last_stats = st
+        return st
+
+    def train(self, numIterations: int, views_per_step: int = 1) -> None:
+        """train(n) (gaussian-renderer.ts:3744-3854): n steps, a seeded
+        random camera per step; stopTraining() ends the loop between steps."""
+        import time
+        if self._training or numIterations <= 0:
+            return
+        self._training, self._stop = True, False
+        self._target_iters = numIterations
+        t0 = time.perf_counter()
+        done = 0
+        try:
+            for _ in range(numIterations):
+                if self._stop:
+                    break
+                st = L.SkyStepStats()
+                L.check(self._L.sky_train(self._h, 1, views_per_step, C.byref(st)))
+                self.last_stats = st
+                done += 1
+        finally:
+            dt = time.perf_counter() - t0
+            self._ips = done / dt if dt > 0 else 0.0
+            self._training, self._stop = False, False
+
+    def stopTraining(self) -> None:
+        if self._training:
+            self._stop = True
+
+    # -- prune / densify / opacity reset -----------------------------------
+    def prune(self, minOpacity: float = 0.005, maxScale: float = float("inf"),
+              max_remove_ratio: float = 0.0, mask: np.ndarray | None = None) -> int:
+        p = L.SkyPruneParams(minOpacity, maxScale, max_remove_ratio, 0)
+        m = None if mask is None else np.ascontiguousarray(mask, dtype=np.uint8)
+        removed = C.c_uint32()
+        L.check(self._L.sky_prune(self._h, C.byref(p), L.ptr(m), C.byref(removed)))
+        return self.getGaussianCount()
+
+    def resetOpacity(self, maxOpacity: float = 0.1) -> None:
+        L.check(self._L.sky_reset_opacity(self._h, maxOpacity))
+
+    # -- parameters and status ---------------------------------------------
+    def getTrainingParams(self) -> TrainingParams:
+        c = self.config
+        return TrainingParams(c.lr_means, c.lr_sh, c.lr_opacity, c.lr_scale, c.lr_rotation,
+                              c.sh_update_interval)
+
+    def setTrainingParams(self, **params) -> None:
+        for k, v in params.items():
+            if k not in TrainingParams.__dataclass_fields__:
+                raise KeyError(k)
+            setattr(self.config, k, v)
+        L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
+
+    def getLossWeights(self) -> LossWeights:
+        return LossWeights(self.config.w_l2, self.config.w_l1, self.config.w_ssim)
+
+    def setLossWeights(self, **w) -> None:
+        for k, v in w.items():
+            if k not in LossWeights.__dataclass_fields__:
+                raise KeyError(k)
+            setattr(self.config, k, v)
+        L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
+
+    def getStatus(self) -> L.SkyStatus:
+        st = L.SkyStatus()
+        L.check(self._L.sky_get_status(self._h, C.byref(st)))
+        return st
+
+    def getTrainingStatus(self) -> TrainingStatus:
+        st = self.getStatus()
+        return TrainingStatus(self._training, int(st.iteration), self._target_iters, self._ips,
+                              int(st.num_gaussians))
+
+    def getGaussianCount(self) -> int:
+        n = C.c_uint32()
+        L.check(self._L.sky_get_count(self._h, C.byref(n)))
+        return n.value
+
+    def params(self) -> np.ndarray:
+        n = self.getGaussianCount()
+        out = np.empty((L.SKY_NUM_PLANES, n), dtype=np.float32)
+        L.check(self._L.sky_get_params(self._h, L.ptr(out), n))
+        return out
+
+    def moments(self):
+        n = self.getGaussianCount()
+        m1 = np.empty((L.SKY_NUM_PLANES, n), dtype=np.float32)
+        m2 = np.empty((L.SKY_NUM_PLANES, n), dtype=np.float32)
+        L.check(self._L.sky_get_moments(self._h, L.ptr(m1), L.ptr(m2), n))
+        return m1, m2
+
+    def read_buffer(self, name: str) -> np.ndarray:
+        which = L.BUF[name]
+        size = C.c_uint64()
+        L.check(self._L.sky_read_buffer(self._h, which, None, 0, C.byref(size)))
+        dt = np.dtype(L.BUF_DTYPE[name])
+        out = np.empty(size.value // dt.itemsize, dtype=dt)
+        if size.value:
+            L.check(self._L.sky_read_buffer(self._h, which, L.ptr(out), size.value, C.byref(size)))
+        return out
+
+    def sync(self) -> None:
+        L.check(self._L.sky_sync(self._h))

@@ -1,0 +1,74 @@
+"""The C-ABI library on a host without a GPU: it loads, exports every entry
+point include/skyfall.h declares, keeps the struct layouts the header
+describes, and reports errors through status codes (no compute calls)."""
+import ctypes as C
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO
+
+
+def header_functions():
+    text = (REPO / "include" / "skyfall.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(sky_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported(sky):
+    L = sky.lib()
+    names = header_functions()
+    assert len(names) >= 25
+    missing = [n for n in names if not hasattr(L, n)]
+    assert not missing, missing
+    # and the Python binding declares a prototype for each of them
+    assert set(names) <= set(sky._lib.PROTOTYPES)
+
+
+def test_config_defaults_are_the_reference_defaults(sky):
+    c = sky.default_config()
+    assert c.struct_size == C.sizeof(sky._lib.SkyConfig)
+    assert (c.tile_size, c.sh_degree_interval, c.sh_update_interval) == (16, 1000, 16)
+    assert (c.near_plane, c.far_plane, c.radius_clip) == (np.float32(0.2), 10000.0, 512.0)
+    assert c.eps2d == np.float32(0.3)
+    assert (c.w_l2, c.w_l1, c.w_ssim) == (0.0, np.float32(0.8), np.float32(0.2))
+    assert c.lr_means == np.float32(0.00016) and c.lr_sh == np.float32(0.0025)
+    assert c.lr_opacity == np.float32(0.025) and c.lr_scale == np.float32(0.005)
+    assert c.lr_rotation == np.float32(0.001)
+    assert (c.beta1, c.beta2, c.adam_eps) == (np.float32(0.9), np.float32(0.999), np.float32(1e-8))
+
+
+def test_config_size_is_checked_before_touching_the_device(sky):
+    L = sky.lib()
+    c = sky.default_config()
+    c.struct_size = 12
+    h = C.c_void_p()
+    assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
+    assert b"SkyConfig size" in L.sky_last_error()
+    c = sky.default_config(tile_size=12)
+    assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
+
+
+def test_pinhole_camera_matches_reference_projection(sky):
+    from skyfall import scenes
+    view = scenes.look_at((1.0, 2.0, -3.0))
+    out = sky._lib.SkyCamera()
+    vp = view.ctypes.data_as(C.c_void_p)
+    assert sky.lib().sky_camera_pinhole(vp, 900.5, 880.25, 955.0, 530.0, 1920, 1080, C.byref(out)) == 0
+    ref = scenes.pinhole(view, 900.5, 880.25, 955.0, 530.0, 1920, 1080)
+    assert np.array_equal(np.ctypeslib.as_array(out.proj), ref["proj"])
+    assert np.array_equal(np.ctypeslib.as_array(out.view), ref["view"])
+    # row 3 of the projection is (0, 0, 1, 0): clip.w = camera-space z
+    P = ref["proj"].reshape(4, 4).T
+    assert np.array_equal(P[3], [0, 0, 1, 0])
+
+
+def test_null_context_and_argument_errors(sky):
+    L = sky.lib()
+    E = sky._lib
+    assert L.sky_get_count(None, None) == E.SKY_ERR_ARG
+    assert L.sky_render(None, None, 0, None, None) == E.SKY_ERR_ARG
+    assert L.sky_destroy(None) == 0
+    assert L.sky_sort_pairs(None, None, None, None, 4, 8, None) == E.SKY_ERR_ARG
+    assert L.sky_version() == 1
