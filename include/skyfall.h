@@ -126,7 +126,22 @@ typedef struct SkyStatus {
   uint32_t capacity;
   uint32_t num_cameras;
   uint32_t error_flags;       /* sticky device error word (0 = none)        */
+  uint64_t kernel_launches;   /* kernels launched by the context so far     */
 } SkyStatus;
+
+/* Stages timed by sky_set_profiling / sky_get_stage_times, in order.  The
+ * reference's TrainingProfiler (src/utils/training-profiler.ts:27-192) times
+ * the same passes with wall clock around queue fences; here each stage is
+ * bracketed by CUDA events on the context's stream.                       */
+#define SKY_STAGE_PREPROCESS 0
+#define SKY_STAGE_SCAN 1
+#define SKY_STAGE_EMIT 2
+#define SKY_STAGE_SORT 3
+#define SKY_STAGE_RANGES 4
+#define SKY_STAGE_FORWARD 5
+#define SKY_STAGE_BACKWARD 6
+#define SKY_STAGE_GEOM_ADAM 7
+#define SKY_NUM_STAGES 8
 
 /* Prune rule of applyMultiViewPrune (gaussian-renderer.ts:2840-2886) with
  * the random budget replaced by a seeded one: prunable if
@@ -224,6 +239,16 @@ int sky_get_count(void* ctx, uint32_t* n);
 int sky_get_status(void* ctx, SkyStatus* st);
 int sky_read_buffer(void* ctx, int which, void* dst, uint64_t bytes, uint64_t* size_out);
 int sky_sync(void* ctx);
+
+/* ---- streams and profiling ------------------------------------------------
+ * sky_get_stream: the cudaStream_t all of the context's work runs on, so a
+ * caller can order its own work (or CUDA events) against it.
+ * sky_set_profiling(1) resets and starts per-stage timing (profiledTrainStep,
+ * gaussian-renderer.ts:3662-3742); sky_get_stage_times returns the summed
+ * milliseconds of SKY_NUM_STAGES stages and the number of timed steps.     */
+int sky_get_stream(void* ctx, void** stream);
+int sky_set_profiling(void* ctx, int enabled);
+int sky_get_stage_times(void* ctx, double* ms, uint32_t n, uint64_t* steps);
 
 /* ---- device-pointer operators --------------------------------------------
  * Stable LSD radix sort of (u32 key, u32 value) pairs on the low key_bits

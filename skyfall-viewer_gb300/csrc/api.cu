@@ -130,6 +130,12 @@ struct Context {
   uint32_t last_items = 0, last_tiles = 0, last_pixels = 0, last_groups = 0;
   bool fwd_ready = false;
   uint32_t error_flags = 0;
+  uint64_t launches = 0;
+  // per-stage profiling (CUDA events on the context's stream)
+  bool profiling = false;
+  cudaEvent_t ev[SKY_NUM_STAGES + 1] = {};
+  double stage_ms[SKY_NUM_STAGES] = {};
+  uint64_t prof_steps = 0;
 };
 
 int dev_alloc(Context* c, Buf& b, size_t bytes, bool keep = false) {
@@ -362,11 +368,20 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   }
   DevBuffers b = make_buffers(c);
   cudaStream_t s = c->stream;
+  const bool prof = c->profiling;
+  auto mark = [&](int k) -> int {
+    if (prof) CK(cudaEventRecord(c->ev[k], s));
+    return SKY_OK;
+  };
+  uint64_t launches = 0;
   CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
+  TRY(mark(0));
   launch_preprocess(b, c->n, nv, s);
+  TRY(mark(1));
   launch_scan(b, (uint32_t)items, s);
   launch_group_bounds(b, s);
+  launches += 5;
   // size the intersection buffers from the device count (the reference reads
   // the projections back for its host cumsum at the same point)
   CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
@@ -378,25 +393,47 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
     CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
     CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
     launch_group_bounds(b, s);
+    ++launches;
   }
+  TRY(mark(2));
   launch_emit(b, c->n, nv, s);
+  TRY(mark(3));
   DevStatus* dst = (DevStatus*)c->d_st.p;
   for (uint32_t g = 0; g < ngroups; ++g) {
     SortSegment seg{&dst->group_bounds[g][0], 0};
     CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap,
                          sp.groups[g].key_bits, c->sort, &dst->error, s));
+    launches += 2 + (sp.groups[g].key_bits + 7) / 8;
   }
+  TRY(mark(4));
   launch_ranges(b, c->icap, s);
+  TRY(mark(5));
   launch_forward(b, (uint32_t)tile_total, ts, with_loss && cfg.w_ssim > 0.0f, nv, max_view_px, s);
   if (with_loss) launch_loss_final(b, s);
+  launches += 4 + (with_loss ? 1 : 0) + (with_loss && cfg.w_ssim > 0.0f ? 1 : 0);
+  TRY(mark(6));
   if (mode >= kBackward) {
     if (ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
     launch_backward(b, (uint32_t)tile_total, ts, ref, s);
+    TRY(mark(7));
     launch_geom_adam(b, c->n, s);
+    launches += 2;
+  } else {
+    TRY(mark(7));
   }
+  TRY(mark(8));
   CK(cudaGetLastError());
   CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
+  c->launches += launches;
+  if (prof) {
+    for (int k = 0; k < SKY_NUM_STAGES; ++k) {
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]));
+      c->stage_ms[k] += ms;
+    }
+    c->prof_steps += 1;
+  }
   c->error_flags |= c->h_st->error;
   if (c->h_st->error & SKY_DEVERR_SORT_TIMEOUT)
     return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
@@ -521,6 +558,8 @@ int sky_destroy(void* p) {
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
                 &c->flag_scan, &c->d_sp, &c->d_st};
   for (Buf* b : all) dev_free(c, *b);
+  for (int k = 0; k <= SKY_NUM_STAGES; ++k)
+    if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->h_sp) cudaFreeHost(c->h_sp);
   if (c->h_st) cudaFreeHost(c->h_st);
   if (c->stream) cudaStreamDestroy(c->stream);
@@ -777,6 +816,7 @@ int sky_get_status(void* p, SkyStatus* st) {
   st->capacity = c->stride;
   st->num_cameras = (uint32_t)c->cams.size();
   st->error_flags = c->error_flags;
+  st->kernel_launches = c->launches;
   return SKY_OK;
 }
 
@@ -842,6 +882,32 @@ int sky_sync(void* p) {
   Context* c = as_ctx(p);
   if (!c) return fail(SKY_ERR_ARG, "null context");
   CK(cudaStreamSynchronize(c->stream));
+  return SKY_OK;
+}
+
+int sky_get_stream(void* p, void** stream) {
+  Context* c = as_ctx(p);
+  if (!c || !stream) return fail(SKY_ERR_ARG, "bad arguments");
+  *stream = (void*)c->stream;
+  return SKY_OK;
+}
+
+int sky_set_profiling(void* p, int enabled) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (enabled && !c->ev[0])
+    for (int k = 0; k <= SKY_NUM_STAGES; ++k) CK(cudaEventCreate(&c->ev[k]));
+  c->profiling = enabled != 0;
+  for (int k = 0; k < SKY_NUM_STAGES; ++k) c->stage_ms[k] = 0.0;
+  c->prof_steps = 0;
+  return SKY_OK;
+}
+
+int sky_get_stage_times(void* p, double* ms, uint32_t n, uint64_t* steps) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  for (uint32_t k = 0; k < n && k < (uint32_t)SKY_NUM_STAGES; ++k) ms[k] = c->stage_ms[k];
+  if (steps) *steps = c->prof_steps;
   return SKY_OK;
 }
 

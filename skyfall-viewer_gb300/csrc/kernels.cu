@@ -28,8 +28,11 @@ SKY_DEV int find_view(const StepParams& sp, uint32_t tile) {
   return v;
 }
 
+// Any error earlier in the step (capacity overflow, a sort that gave up, keys
+// out of order) makes every later kernel of the step a no-op, so no kernel
+// indexes with data that failed its checks.
 SKY_DEV bool capacity_failed(const DevStatus* st) {
-  return (*(volatile const uint32_t*)&st->error & SKY_DEVERR_CAPACITY) != 0u;
+  return *(volatile const uint32_t*)&st->error != 0u;
 }
 
 // ---------------------------------------------------------------------------
@@ -203,6 +206,10 @@ __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
   const GroupInfo& gi = sp.groups[g];
   const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
   const uint32_t t = gi.tile_begin + (b.keys_sorted[i] >> 16);
+  if (t >= gi.tile_end || (i > gb && gi.tile_begin + (b.keys_sorted[i - 1] >> 16) > t)) {
+    atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);  // unsorted or corrupt keys
+    return;
+  }
   if (i == gb) {
     for (uint32_t u = gi.tile_begin; u <= t; ++u) b.offsets[u] = i;
   } else {

@@ -24,6 +24,13 @@ __device__ __forceinline__ uint32_t lanemask_lt() {
   return m;
 }
 
+// Mask of digit `pass`: 8 bits, fewer in the last pass when key_bits is not
+// a multiple of 8 (bits above key_bits do not take part in the order).
+__device__ __forceinline__ uint32_t digit_mask(uint32_t key_bits, int pass) {
+  const int left = (int)key_bits - 8 * pass;
+  return left >= 8 ? 0xFFu : ((1u << left) - 1u);
+}
+
 __device__ __forceinline__ void seg_bounds(const SortSegment& s, uint32_t& b, uint32_t& n) {
   if (s.bounds) {
     b = s.bounds[0];
@@ -38,7 +45,7 @@ __device__ __forceinline__ void seg_bounds(const SortSegment& s, uint32_t& b, ui
 // Digit counts of every pass in one read of the keys; also clears the
 // look-back words of the tiles this segment will use.
 __global__ void __launch_bounds__(kSortThreads)
-k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes,
+k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, uint32_t key_bits,
             uint32_t* __restrict__ hist, uint32_t* __restrict__ lookback, uint32_t max_tiles) {
   __shared__ uint32_t s_hist[kMaxPasses][kRadix];
   for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kSortThreads) (&s_hist[0][0])[i] = 0;
@@ -63,7 +70,7 @@ k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes,
     uint32_t active = __ballot_sync(0xFFFFFFFFu, valid);
     if (valid) {
       for (int p = 0; p < passes; ++p) {
-        uint32_t d = (k >> (8 * p)) & 0xFFu;
+        uint32_t d = (k >> (8 * p)) & digit_mask(key_bits, p);
         uint32_t peers = __match_any_sync(active, d);
         if ((peers & lanemask_lt()) == 0) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
       }
@@ -98,7 +105,8 @@ __global__ void __launch_bounds__(kRadix) k_sort_scan(uint32_t* __restrict__ his
 __global__ void __launch_bounds__(kSortThreads)
 k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
            uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, SortSegment seg,
-           int pass, const uint32_t* __restrict__ hist, uint32_t* __restrict__ tile_counter,
+           int pass, uint32_t key_bits, const uint32_t* __restrict__ hist,
+           uint32_t* __restrict__ tile_counter,
            uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_keys[kSortTile];
   __shared__ uint32_t s_vals[kSortTile];
@@ -118,6 +126,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
   const uint32_t base = tile * (uint32_t)kSortTile;
   if (base >= n) return;
   const int shift = 8 * pass;
+  const uint32_t dmask = digit_mask(key_bits, pass);
 
   uint32_t key[kSortItems], val[kSortItems], rank[kSortItems];
   const uint32_t lt = lanemask_lt();
@@ -132,7 +141,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
   for (int k = 0; k < kSortItems; ++k) {
     uint32_t idx = base + warp * (32 * kSortItems) + k * 32 + lane;
     bool valid = idx < n;
-    uint32_t d = (key[k] >> shift) & 0xFFu;
+    uint32_t d = (key[k] >> shift) & dmask;
     uint32_t active = __ballot_sync(0xFFFFFFFFu, valid);
     uint32_t peers = 0, cnt = 0;
     if (valid) {
@@ -201,7 +210,7 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
 #pragma unroll
   for (int k = 0; k < kSortItems; ++k) {
     if (rank[k] != 0xFFFFFFFFu) {
-      uint32_t dk = (key[k] >> shift) & 0xFFu;
+      uint32_t dk = (key[k] >> shift) & dmask;
       uint32_t lp = s_block_excl[dk] + s_warp_hist[warp][dk] + rank[k];
       s_keys[lp] = key[k];
       s_vals[lp] = val[k];
@@ -211,8 +220,12 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
   const uint32_t cnt = min((uint32_t)kSortTile, n - base);
   for (uint32_t i = tid; i < cnt; i += kSortThreads) {
     uint32_t kk = s_keys[i];
-    uint32_t dk = (kk >> shift) & 0xFFu;
+    uint32_t dk = (kk >> shift) & dmask;
     uint32_t gp = s_global[dk] + (i - s_block_excl[dk]);
+    if (gp >= n) {  // only after a timed-out look-back; never write out of range
+      atomicOr(err, SKY_DEVERR_SORT_TIMEOUT);
+      continue;
+    }
     keys_out[begin + gp] = kk;
     vals_out[begin + gp] = s_vals[i];
   }
@@ -227,7 +240,7 @@ size_t sort_scratch_bytes(uint32_t max_n) {
   b += 256;                                        // tile counters (padded)
   b += (size_t)kMaxPasses * tiles * kRadix * 4;    // look-back
   b += (size_t)(max_n + 64) * 4 * 2;               // ping-pong
-  return b + 1024;
+  return b + 4096;                                 // 256-byte alignment of 5 pieces
 }
 
 SortScratch sort_scratch_carve(void* base, uint32_t max_n) {
@@ -262,7 +275,7 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
   uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
   if (tiles == 0) tiles = 1;
   uint32_t hist_blocks = tiles < 1024u ? tiles : 1024u;
-  k_sort_hist<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, seg, passes, sc.hist,
+  k_sort_hist<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, seg, passes, key_bits, sc.hist,
                                                          sc.lookback, sc.max_tiles);
   k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist);
   const uint32_t* src_k = keys_in;
@@ -271,7 +284,7 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
     bool to_out = ((passes - 1 - p) % 2) == 0;
     uint32_t* dk = to_out ? keys_out : sc.keys_tmp;
     uint32_t* dv = to_out ? vals_out : sc.vals_tmp;
-    k_onesweep<<<tiles, kSortThreads, 0, stream>>>(src_k, src_v, dk, dv, seg, p, sc.hist,
+    k_onesweep<<<tiles, kSortThreads, 0, stream>>>(src_k, src_v, dk, dv, seg, p, key_bits, sc.hist,
                                                     sc.tile_counter, sc.lookback, sc.max_tiles,
                                                     err);
     src_k = dk;

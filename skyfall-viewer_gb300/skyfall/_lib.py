@@ -86,7 +86,10 @@ class SkyStatus(C.Structure):
     _fields_ = [("iteration", C.c_uint64), ("adam_steps", C.c_uint64),
                 ("last_intersections", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("num_gaussians", C.c_uint32), ("capacity", C.c_uint32), ("num_cameras", C.c_uint32),
-                ("error_flags", C.c_uint32)]
+                ("error_flags", C.c_uint32), ("kernel_launches", C.c_uint64)]
+
+
+STAGES = ["preprocess", "scan", "emit", "sort", "ranges", "forward", "backward", "geom_adam"]
 
 
 class SkyPruneParams(C.Structure):
@@ -136,6 +139,9 @@ PROTOTYPES = {
     "sky_read_buffer": (I32, [P, I32, P, U64, C.POINTER(U64)]),
     "sky_sync": (I32, [P]),
     "sky_sort_pairs": (I32, [P, P, P, P, U32, U32, P]),
+    "sky_get_stream": (I32, [P, C.POINTER(C.c_void_p)]),
+    "sky_set_profiling": (I32, [P, I32]),
+    "sky_get_stage_times": (I32, [P, C.POINTER(C.c_double), U32, C.POINTER(U64)]),
 }
 
 LIB_PATH = Path(__file__).resolve().parent / "libskyfall.so"

@@ -257,3 +257,19 @@ class GaussianRenderer:
 
     def sync(self) -> None:
         L.check(self._L.sky_sync(self._h))
+
+    # -- profiling (profiledTrainStep / TrainingProfiler) -------------------
+    def stream(self) -> int:
+        s = C.c_void_p()
+        L.check(self._L.sky_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def enableProfiling(self, enabled: bool = True) -> None:
+        L.check(self._L.sky_set_profiling(self._h, int(enabled)))
+
+    def stageTimes(self) -> tuple[dict, int]:
+        """Summed milliseconds per stage and the number of timed steps."""
+        arr = (C.c_double * len(L.STAGES))()
+        steps = C.c_uint64()
+        L.check(self._L.sky_get_stage_times(self._h, arr, len(L.STAGES), C.byref(steps)))
+        return dict(zip(L.STAGES, list(arr))), steps.value
