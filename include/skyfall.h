@@ -167,7 +167,9 @@ typedef struct SkyDensifyParams {
 } SkyDensifyParams;
 
 /* ---- buffers readable with sky_read_buffer (introspection) -------------- */
-#define SKY_BUF_RECORDS 1      /* per (view, Gaussian) projection record, 12 f32 */
+#define SKY_BUF_RECORDS 1      /* per (view, Gaussian) raster record, 12 f32:
+                                  mean x, y, conic a, b, c, opacity, colour r,
+                                  g, b, alpha-skip bound on s, box half-widths */
 #define SKY_BUF_COUNTS 2       /* per (view, Gaussian) tile count, u32            */
 #define SKY_BUF_CUMSUM 3       /* inclusive scan of the counts, u32               */
 #define SKY_BUF_KEYS_EMIT 4    /* keys in emission order, u32                     */
@@ -183,6 +185,7 @@ typedef struct SkyDensifyParams {
 #define SKY_BUF_TILE_GRADS 14  /* reference mode: 54 i32 per sorted intersection  */
 #define SKY_BUF_GRADS 15       /* 59 gradient planes of the last backward         */
 #define SKY_BUF_GROUPS 16      /* per sort group: begin, end intersection, u32    */
+#define SKY_BUF_DEPTH_RADIUS 18 /* per (view, Gaussian) camera depth, radius, f32 */
 #define SKY_BUF_STEP_SCALARS 17 /* f32: lr pos, scale, rot, opacity, sh, beta1,
                                    beta2, eps, bias-correction 1/bc1, 1/sqrt(bc2),
                                    SH degree, SH-update flag                     */

@@ -651,7 +651,9 @@ int orc_loss(const float* rgba, const float* target, const OrcCam* cam_in,
       }
       if (s.w_ssim > 0.0f) {
         // computeSSIMGrad (training-loss.wgsl:33-84)
-        const float C1 = 0.01f * 0.01f, C2 = 0.03f * 0.03f, nwin = 25.0f;
+        // WGSL const-expressions 0.01 * 0.01 and 0.03 * 0.03 are evaluated
+        // exactly and rounded to f32 once.
+        const float C1 = 0.0001f, C2 = 0.0009f, nwin = 25.0f;
         for (int c = 0; c < 3; ++c) {
           float mx = 0.0f, my = 0.0f;
           for (int dy = -2; dy <= 2; ++dy)

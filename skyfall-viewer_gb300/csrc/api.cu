@@ -109,7 +109,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   uint32_t n = 0, stride = 0;
   Buf params, m1, m2, grads, tmp_planes;
-  Buf records, counts, rects, cumsum, block_sums;
+  Buf records, aux, counts, rects, cumsum, block_sums;
   Buf keys, keys_sorted, vals_sorted, rec_of, flatten, partials, tile_grads, gsum54;
   Buf offsets, loss_partials, color, alpha, tfinal, last, residual, targets, sort_mem;
   Buf flags, flag_scan, d_sp, d_st;
@@ -176,6 +176,7 @@ DevBuffers make_buffers(Context* c) {
   b.m2 = (float*)c->m2.p;
   b.grads = (float*)c->grads.p;
   b.records = (float4*)c->records.p;
+  b.aux = (float2*)c->aux.p;
   b.counts = (uint32_t*)c->counts.p;
   b.rects = (uint2*)c->rects.p;
   b.cumsum = (uint32_t*)c->cumsum.p;
@@ -307,6 +308,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   if (items >= (1ull << 32)) return fail(SKY_ERR_ARG, "views x Gaussians exceeds 2^32");
   // buffers
   TRY(dev_alloc(c, c->records, items * 48));
+  TRY(dev_alloc(c, c->aux, items * 8));
   TRY(dev_alloc(c, c->counts, items * 4));
   TRY(dev_alloc(c, c->rects, items * 8));
   TRY(dev_alloc(c, c->cumsum, items * 4));
@@ -551,7 +553,7 @@ int sky_destroy(void* p) {
   Context* c = as_ctx(p);
   if (!c) return SKY_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
-  Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records,
+  Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records, &c->aux,
                 &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->keys,
                 &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->partials,
                 &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,
@@ -829,6 +831,7 @@ int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* siz
   uint64_t sz = 0, pitch_src = 0, rows = 0, row_bytes = 0;
   switch (which) {
     case SKY_BUF_RECORDS: src = c->records.p; sz = items * 48; break;
+    case SKY_BUF_DEPTH_RADIUS: src = c->aux.p; sz = items * 8; break;
     case SKY_BUF_COUNTS: src = c->counts.p; sz = items * 4; break;
     case SKY_BUF_CUMSUM: src = c->cumsum.p; sz = items * 4; break;
     case SKY_BUF_KEYS_EMIT: src = c->keys.p; sz = I * 4; break;

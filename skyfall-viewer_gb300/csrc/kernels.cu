@@ -51,14 +51,27 @@ __global__ void __launch_bounds__(256) k_preprocess(DevBuffers b) {
   const bool ok = project_gaussian(get, vi, sp, (int)sp.sh_deg, true, o);
   const size_t item = (size_t)v * sp.n + g;
   // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
-  // whatever the rounding of exp, so skipping it there decides as the
-  // reference does.
-  float smax = -1.0f;
-  if (ok) smax = __logf(255.0f * o.opacity) + 1e-3f;
+  // whatever the rounding of exp (|error| < 1e-6 << 1e-3), so skipping it
+  // there decides as the reference does.  The pixels with s <= smax lie in
+  // the ellipse d^T conic d <= 2 smax, whose bounding box has half-widths
+  // sqrt(2 smax cov00), sqrt(2 smax cov11).  The f32 evaluation of s has a
+  // relative error below 20 ulp x cond(conic) <= 0.12 (cond <= 1e5 because
+  // eps2d >= 0.3 and radius <= 512), so the box is computed for
+  // 1.25 smax + 0.01: no pixel it excludes can pass the alpha test.
+  float smax = -1.0f, hx = -1.0f, hy = -1.0f;
+  if (ok) {
+    smax = __logf(255.0f * o.opacity) + 1e-3f;
+    if (smax > 0.0f) {
+      const float sb = 2.0f * (1.25f * smax + 0.01f);
+      hx = sqrtf(sb * o.cov00) + 0.01f;
+      hy = sqrtf(sb * o.cov11) + 0.01f;
+    }
+  }
   float4* rec = b.records + item * 3;
   rec[0] = make_float4(o.mx, o.my, o.ca, o.cb);
   rec[1] = make_float4(o.cc, o.opacity, o.col[0], o.col[1]);
-  rec[2] = make_float4(o.col[2], o.depth, o.radius, smax);
+  rec[2] = make_float4(o.col[2], smax, hx, hy);
+  b.aux[item] = make_float2(o.depth, o.radius);
   b.counts[item] = o.count;
   b.rects[item] = make_uint2(o.x0 | (o.y0 << 16), o.x1 | (o.y1 << 16));
 }
@@ -175,7 +188,7 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const ViewInfo& vi = sp.views[v];
   const uint2 rc = b.rects[item];
   const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
-  const float depth = b.records[item * 3 + 2].y;
+  const float depth = b.aux[item].x;
   const uint32_t dq = wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
   const uint32_t it = (uint32_t)item;
   for (uint32_t ty = y0; ty < y1; ++ty)
@@ -244,11 +257,35 @@ __global__ void k_ranges_empty(DevBuffers b) {
 // ---------------------------------------------------------------------------
 constexpr int kFwdBatch = 256;
 
+// Bit w set when warp w of the tile (pixel rows [w * 32/TS, (w + 1) * 32/TS))
+// has a pixel centre inside the splat's alpha >= 1/255 bounding box
+// (half-widths r2.z, r2.w around the mean r0.xy; negative = no pixel).
+template <int TS>
+SKY_DEV uint32_t warp_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
+  constexpr int RPW = 32 / TS;
+  const float hx = r2.z, hy = r2.w;
+  if (!(hx > 0.0f) || !(hy > 0.0f)) return 0u;
+  const float cx0 = (float)x0 + 0.5f, cx1 = (float)x0 + ((float)TS - 0.5f);
+  if (cx1 < r0.x - hx || cx0 > r0.x + hx) return 0u;
+  const float ylo = r0.y - hy - (float)y0 - 0.5f;  // rows r with r >= ylo ...
+  const float yhi = r0.y + hy - (float)y0 - 0.5f;  // ... and r <= yhi
+  if (!(yhi >= 0.0f) || !(ylo <= (float)(TS - 1))) return 0u;
+  const int rlo = ylo <= 0.0f ? 0 : (int)ceilf(ylo);
+  const int rhi = yhi >= (float)(TS - 1) ? TS - 1 : (int)floorf(yhi);
+  if (rlo > rhi) return 0u;
+  const int wlo = rlo / RPW, whi = rhi / RPW;
+  const uint32_t upto = whi >= 31 ? 0xFFFFFFFFu : ((1u << (whi + 1)) - 1u);
+  return upto & ~((1u << wlo) - 1u);
+}
+
 template <int TS>
 __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   constexpr int NT = TS * TS;
+  constexpr int NW = NT / 32;
   __shared__ float4 s_rec[kFwdBatch * 3];
-  __shared__ double s_loss[NT / 32];
+  __shared__ uint32_t s_mask[kFwdBatch];
+  __shared__ uint8_t s_list[NW][kFwdBatch];
+  __shared__ double s_loss[NW];
   const StepParams& sp = *b.sp;
   const uint32_t tile = blockIdx.x;
   if (tile >= sp.num_tiles) return;
@@ -257,27 +294,45 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   const ViewInfo& vi = sp.views[v];
   const uint32_t local = tile - vi.tile_base;
   const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
-  const uint32_t tid = threadIdx.x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t x = tx * TS + (tid % TS), y = ty * TS + (tid / TS);
   const bool inside = x < vi.width && y < vi.height;
   const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
   const float pxf = (float)x + 0.5f, pyf = (float)y + 0.5f;
   float C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, A = 0.0f, Tp = 1.0f;
-  uint32_t last = start;
+  // the reference's loop visits every intersection of the tile up to the
+  // one that ends it (training-forward-tiles.wgsl:168-207)
+  uint32_t last = end - 1;
   bool done = !inside;
+  const uint32_t wbit = 1u << warp;
+  const uint32_t lt = (1u << lane) - 1u;
   for (uint32_t bs = start; bs < end; bs += kFwdBatch) {
     const uint32_t cnt = min((uint32_t)kFwdBatch, end - bs);
     __syncthreads();
     for (uint32_t k = tid; k < cnt; k += NT) {
       const size_t r = b.flatten[bs + k];
-      s_rec[k * 3 + 0] = b.records[r * 3 + 0];
+      const float4 q0 = b.records[r * 3 + 0];
+      const float4 q2 = b.records[r * 3 + 2];
+      s_rec[k * 3 + 0] = q0;
       s_rec[k * 3 + 1] = b.records[r * 3 + 1];
-      s_rec[k * 3 + 2] = b.records[r * 3 + 2];
+      s_rec[k * 3 + 2] = q2;
+      s_mask[k] = warp_mask<TS>(q0, q2, tx * TS, ty * TS);
     }
     __syncthreads();
+    // this warp's splats of the batch, in order (skipped splats cannot pass
+    // the alpha test at any pixel of the warp)
+    uint32_t nlist = 0;
+    for (uint32_t base = 0; base < cnt; base += 32) {
+      const uint32_t j = base + lane;
+      const bool in = j < cnt && (s_mask[j] & wbit);
+      const uint32_t m = __ballot_sync(kFull, in);
+      if (in) s_list[warp][nlist + __popc(m & lt)] = (uint8_t)j;
+      nlist += __popc(m);
+    }
+    __syncwarp();
     if (!done) {
-      for (uint32_t j = 0; j < cnt; ++j) {
-        last = bs + j;
+      for (uint32_t li = 0; li < nlist; ++li) {
+        const uint32_t j = s_list[warp][li];
         const float4 r0 = s_rec[j * 3 + 0];
         const float4 r2 = s_rec[j * 3 + 2];
         const float dx = pxf - r0.x, dy = pyf - r0.y;
@@ -286,7 +341,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
         const float s2 = (r1.x * dy) * dy;
         float so2 = 0.5f * (s1 + s2);
         so2 = so2 + (r0.w * dx) * dy;
-        if (so2 < 0.0f || so2 > r2.w) continue;
+        if (so2 < 0.0f || so2 > r2.y) continue;
         const float G = sky_expf(-so2);
         const float al = r1.y * G;
         const float a = fmin_(al, MAX_ALPHA);
@@ -299,6 +354,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
         A = A + ca;
         Tp = Tp * (1.0f - a);
         if (1.0f - A < T_THRESH) {
+          last = bs + j;
           done = true;
           break;
         }
@@ -368,7 +424,7 @@ __global__ void __launch_bounds__(256) k_ssim(DevBuffers b) {
     yy = min(max(yy, 0), H - 1);
     return b.targets[(size_t)vi.target_base + (size_t)yy * W + xx];
   };
-  const float C1 = 0.01f * 0.01f, C2 = 0.03f * 0.03f, nwin = 25.0f;
+  const float C1 = 0.0001f, C2 = 0.0009f, nwin = 25.0f;  // f32(0.01^2), f32(0.03^2)
   float out[3];
   for (int c = 0; c < 3; ++c) {
     auto comp = [c](float4 f) { return c == 0 ? f.x : (c == 1 ? f.y : f.z); };
@@ -430,22 +486,64 @@ __global__ void __launch_bounds__(1024) k_loss_final(DevBuffers b) {
 // splats back to front from its last contributor, recomputing transmittance
 // from the final product transmittance (T_before = T / (1 - alpha); the
 // product keeps relative precision where 1 - alpha_final would cancel); per
-// pair it forms the
-// nine quantities of backward-tiles-local.wgsl:333-359 (dL/dcolour replaces
-// the 48 SH products: the SH chain is applied once per Gaussian later).
-// Each batch's per-pair values are reduced over the warp with a fixed
-// butterfly, then over the warps in index order, and written per
-// intersection to partials[emission index] -- so every Gaussian's partials
-// are contiguous and the later per-Gaussian sum has a fixed order.
+// pair it forms the nine quantities of backward-tiles-local.wgsl:333-359
+// (dL/dcolour replaces the 48 SH products: the SH chain is applied once per
+// Gaussian later).  A warp skips a splat whose alpha >= 1/255 box misses all
+// of its pixels or that lies beyond all of its pixels' last contributors.
+// Each batch's per-pair values are reduced over the warp by a fixed
+// reduce-scatter (12 shuffles for 9 values), then over the warps in index
+// order, and written per intersection to partials[emission index] -- so
+// every Gaussian's partials are contiguous and the later per-Gaussian sum
+// has a fixed order.
 // ---------------------------------------------------------------------------
+
+// Sum of v[0..8] over the warp, scattered: on return the lane with bit 0
+// clear and slot() == k holds the warp total of v[k] (slot() >= 9: none).
+SKY_DEV float warp_reduce_scatter9(const float v[9], uint32_t lane) {
+  const bool b4 = lane & 16u, b3 = lane & 8u, b2 = lane & 4u, b1 = lane & 2u;
+  float w[5];
+#pragma unroll
+  for (int i = 0; i < 5; ++i) {
+    const float lo = v[i], hi = (i + 5 < 9) ? v[i + 5] : 0.0f;
+    w[i] = (b4 ? hi : lo) + __shfl_xor_sync(kFull, b4 ? lo : hi, 16);
+  }
+  float x3[3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float lo = w[i], hi = (i + 3 < 5) ? w[i + 3] : 0.0f;
+    x3[i] = (b3 ? hi : lo) + __shfl_xor_sync(kFull, b3 ? lo : hi, 8);
+  }
+  float y2[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i) {
+    const float lo = x3[i], hi = (i + 2 < 3) ? x3[i + 2] : 0.0f;
+    y2[i] = (b2 ? hi : lo) + __shfl_xor_sync(kFull, b2 ? lo : hi, 4);
+  }
+  float z = (b1 ? y2[1] : y2[0]) + __shfl_xor_sync(kFull, b1 ? y2[0] : y2[1], 2);
+  return z + __shfl_xor_sync(kFull, z, 1);
+}
+
+// Value index a lane holds after warp_reduce_scatter9, or 9 for none.
+SKY_DEV int scatter9_slot(uint32_t lane) {
+  if (lane & 1u) return 9;
+  const int xi = (int)(((lane >> 2) & 1u) * 2 + ((lane >> 1) & 1u));  // x3 index, 3 = pad
+  if (xi >= 3) return 9;
+  const int wi = (int)((lane >> 3) & 1u) * 3 + xi;                     // w index, >= 5 = pad
+  if (wi >= 5) return 9;
+  const int vi = (int)((lane >> 4) & 1u) * 5 + wi;
+  return vi < 9 ? vi : 9;
+}
+
 template <int TS>
 __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
   constexpr int NT = TS * TS;
   constexpr int NW = NT / 32;
   constexpr int kBwdBatch = NW <= 8 ? 64 : 16;
   __shared__ float4 s_rec[kBwdBatch * 3];
+  __shared__ uint32_t s_mask[kBwdBatch];
   __shared__ float s_part[NW][kBwdBatch][9];
   __shared__ int s_hi[NW];
+  __shared__ uint8_t s_list[NW][kBwdBatch];
   const StepParams& sp = *b.sp;
   const uint32_t tile = blockIdx.x;
   if (tile >= sp.num_tiles) return;
@@ -471,13 +569,16 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
     const float4 rs = b.residual[p];
     r0 = rs.x; r1 = rs.y; r2 = rs.z;
   }
-  int hi = myhi;
+  int whi = myhi;
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) hi = max(hi, __shfl_xor_sync(kFull, hi, o));
-  if (lane == 0) s_hi[warp] = hi;
+  for (int o = 16; o > 0; o >>= 1) whi = max(whi, __shfl_xor_sync(kFull, whi, o));
+  if (lane == 0) s_hi[warp] = whi;
   __syncthreads();
-  hi = s_hi[0];
+  int hi = s_hi[0];
   for (int w = 1; w < NW; ++w) hi = max(hi, s_hi[w]);
+  const int slot = scatter9_slot(lane);
+  const uint32_t wbit = 1u << warp;
+  const uint32_t lt = (1u << lane) - 1u;
   // intersections no pixel reaches get zero partials
   for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
     float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
@@ -490,12 +591,27 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
     __syncthreads();
     for (int k = (int)tid; k < cnt; k += NT) {
       const size_t r = b.flatten[bhi - k];
-      s_rec[k * 3 + 0] = b.records[r * 3 + 0];
+      const float4 q0 = b.records[r * 3 + 0];
+      const float4 q2 = b.records[r * 3 + 2];
+      s_rec[k * 3 + 0] = q0;
       s_rec[k * 3 + 1] = b.records[r * 3 + 1];
-      s_rec[k * 3 + 2] = b.records[r * 3 + 2];
+      s_rec[k * 3 + 2] = q2;
+      s_mask[k] = warp_mask<TS>(q0, q2, tx * TS, ty * TS);
     }
     __syncthreads();
-    for (int j = 0; j < cnt; ++j) {
+    // this warp's splats of the batch (box overlaps a pixel of the warp and
+    // some pixel of the warp has not stopped before it), back to front
+    uint32_t nlist = 0;
+    for (int base = 0; base < cnt; base += 32) {
+      const int j = base + (int)lane;
+      const bool in = j < cnt && (s_mask[j] & wbit) && bhi - j <= whi;
+      const uint32_t m = __ballot_sync(kFull, in);
+      if (in) s_list[warp][nlist + __popc(m & lt)] = (uint8_t)j;
+      nlist += __popc(m);
+    }
+    __syncwarp();
+    for (uint32_t li = 0; li < nlist; ++li) {
+      const int j = s_list[warp][li];
       const int i = bhi - j;
       float val[9];
 #pragma unroll
@@ -508,7 +624,7 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
         const float s2 = (q1.x * dy) * dy;
         float so2 = 0.5f * (s1 + s2);
         so2 = so2 + (q0.w * dx) * dy;
-        if (so2 >= 0.0f && so2 <= q2.w) {
+        if (so2 >= 0.0f && so2 <= q2.y) {
           const float G = sky_expf(-so2);
           const float op = q1.y;
           const float al = op * G;
@@ -547,29 +663,23 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
           }
         }
       }
-      if (__any_sync(kFull, contrib)) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) {
-          float s = val[k];
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) s = s + __shfl_xor_sync(kFull, s, o);
-          val[k] = s;
-        }
-      }
-      if (lane == 0) {
-#pragma unroll
-        for (int k = 0; k < 9; ++k) s_part[warp][j][k] = val[k];
-      }
+      float tot = 0.0f;
+      if (__any_sync(kFull, contrib)) tot = warp_reduce_scatter9(val, lane);
+      if (slot < 9) s_part[warp][j][slot] = tot;
     }
     __syncthreads();
     for (int j = (int)tid; j < cnt; j += NT) {
+      const int i = bhi - j;
+      const uint32_t m = s_mask[j];
       float sum[9];
 #pragma unroll
-      for (int k = 0; k < 9; ++k) sum[k] = s_part[0][j][k];
-      for (int w = 1; w < NW; ++w)
+      for (int k = 0; k < 9; ++k) sum[k] = 0.0f;
+      for (int w = 0; w < NW; ++w) {
+        if (!((m >> w) & 1u) || i > s_hi[w]) continue;  // warp w skipped this splat
 #pragma unroll
         for (int k = 0; k < 9; ++k) sum[k] = sum[k] + s_part[w][j][k];
-      float4* dst = b.partials + (size_t)b.vals_sorted[bhi - j] * kPartialF4;
+      }
+      float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
       dst[0] = make_float4(sum[0], sum[1], sum[2], sum[3]);
       dst[1] = make_float4(sum[4], sum[5], sum[6], sum[7]);
       dst[2] = make_float4(sum[8], 0.0f, 0.0f, 0.0f);
@@ -661,7 +771,7 @@ __global__ void __launch_bounds__(TS* TS) k_backward_ref(DevBuffers b) {
         const float s2 = (q1.x * dy) * dy;
         float so2 = 0.5f * (s1 + s2);
         so2 = so2 + (q0.w * dx) * dy;
-        if (so2 >= 0.0f && so2 <= q2.w) {
+        if (so2 >= 0.0f && so2 <= q2.y) {
           const float G = sky_expf(-so2);
           const float op = q1.y;
           const float a = fmin_(op * G, MAX_ALPHA);

@@ -18,6 +18,7 @@ struct ProjOut {
   float raw[3];          // colour before the clamp
   float dir[3];          // normalize(-p_cam)
   float depth, radius;
+  float cov00, cov11;    // diagonal of the 2D covariance (with eps2d)
   float pc[4];           // camera-space position
   uint32_t count, x0, y0, x1, y1;
 };
@@ -127,6 +128,8 @@ SKY_DEV bool project_gaussian(Get get, const ViewInfo& vi, const StepParams& sp,
   const float radius = ceilf(3.0f * sqrtf(fmax_(l1, l2)));
   if (radius > sp.radius_clip || radius < 1.0f) return false;
   const float det_inv = 1.0f / det;
+  o.cov00 = c00;
+  o.cov11 = c11;
   o.ca = c11 * det_inv;
   o.cb = (-c01) * det_inv;
   o.cc = c00 * det_inv;

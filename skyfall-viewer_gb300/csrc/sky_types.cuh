@@ -71,7 +71,8 @@ struct DevBuffers {
   float* m1;
   float* m2;
   float* grads;
-  float4* records;    // 3 float4 per (view, Gaussian) item
+  float4* records;    // 3 float4 per (view, Gaussian) item: raster record
+  float2* aux;        // depth, radius per item
   uint32_t* counts;   // tiles per item
   uint2* rects;       // packed tile rectangle per item
   uint32_t* cumsum;   // inclusive scan of counts

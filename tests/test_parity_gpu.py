@@ -44,9 +44,11 @@ def check_view(r, ref, n, view_index, tile_base, item_base, isect_base):
     counts = r.read_buffer("counts")[item_base:item_base + n]
     pr = ref["pr"]
     assert np.array_equal(counts, pr["counts"])
+    dr = r.read_buffer("depth_radius").reshape(-1, 2)[item_base:item_base + n]
     vis = pr["rec"][:, 10] > 0
-    assert np.array_equal(rec[:, :11][vis], pr["rec"][:, :11][vis])
-    assert np.all(rec[~vis][:, 10] == 0)
+    assert np.array_equal(rec[:, :9][vis], pr["rec"][:, :9][vis])
+    assert np.array_equal(dr[vis], pr["rec"][:, 9:11][vis])
+    assert np.all(dr[~vis] == 0)
     tl = ref["tl"]
     I = tl["keys_sorted"].shape[0]
     ks = r.read_buffer("keys_sorted")[isect_base:isect_base + I]
