@@ -239,7 +239,7 @@ def main():
     P, cams = workload(args)
     targets = render_targets(sky, cams, args)
     cfg = dict(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0,
-               max_views_per_step=args.views)
+               max_views_per_step=args.views, use_graph=1)
     r = sky.GaussianRenderer(**cfg)
     r.load_points(P)
     r.setTrainingCameras(cams)
@@ -273,6 +273,10 @@ def main():
 
     plain = None
     if not args.no_plain:
+        # the plain per-view path: one view and one Adam step per sky_step,
+        # launched directly with the host-side sizing read-back
+        r.config.use_graph = 0
+        sky._lib.check(r._L.sky_set_config(r._h, sky._lib.C.byref(r.config)))
         psets = [[k % C] for k in range(args.steps * B)]
         for k in range(args.warmup):
             r.trainStep([k % C])

@@ -103,6 +103,17 @@ struct Buf {
   size_t bytes = 0;
 };
 
+// Launch geometry of one pass.  Direct passes size the grids for the step;
+// a captured graph sizes them for the largest step it may replay (kernels
+// read the actual counts from the step parameters and exit early).
+struct Shape {
+  uint32_t nv = 0, n = 0, stride = 0, mode = 0, icap = 0;
+  uint32_t max_tiles = 0, max_view_px = 0, ngroups = 0;
+  uint32_t key_bits[kMaxGroups] = {};
+  bool with_loss = false, ssim = false, ref = false, prof = false;
+  bool same(const Shape& o) const { return memcmp(this, &o, sizeof(Shape)) == 0; }
+};
+
 struct Context {
   SkyConfig cfg{};
   int device = 0;
@@ -136,6 +147,11 @@ struct Context {
   cudaEvent_t ev[SKY_NUM_STAGES + 1] = {};
   double stage_ms[SKY_NUM_STAGES] = {};
   uint64_t prof_steps = 0;
+  // captured training step (use_graph)
+  cudaGraphExec_t gexec = nullptr;
+  Shape gshape;
+  bool gvalid = false;
+  uint64_t graph_launches = 0, graph_captures = 0, warm_steps = 0;
 };
 
 int dev_alloc(Context* c, Buf& b, size_t bytes, bool keep = false) {
@@ -156,6 +172,7 @@ int dev_alloc(Context* c, Buf& b, size_t bytes, bool keep = false) {
     cudaFree(b.p);
     c->device_bytes -= b.bytes;
   }
+  c->gvalid = false;  // a captured graph holds the old pointer
   b.p = p;
   b.bytes = want;
   c->device_bytes += want;
@@ -163,7 +180,10 @@ int dev_alloc(Context* c, Buf& b, size_t bytes, bool keep = false) {
 }
 
 void dev_free(Context* c, Buf& b) {
-  if (b.p) cudaFree(b.p);
+  if (b.p) {
+    cudaFree(b.p);
+    c->gvalid = false;
+  }
   c->device_bytes -= b.bytes;
   b.p = nullptr;
   b.bytes = 0;
@@ -244,6 +264,80 @@ double position_lr(const SkyConfig& cfg, uint64_t iteration) {
   return log_lerp * delay;
 }
 
+// Enqueues the pass on the context's stream.  With sizing_sync (direct
+// passes only) the intersection count is read back after the scan and the
+// buffers grown before emission, as the reference does with its host cumsum.
+int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
+  cudaStream_t s = c->stream;
+  DevBuffers b = make_buffers(c);
+  const bool prof = sh.prof;
+  const bool capturing = !sizing_sync;
+  auto mark = [&](int k) -> int {
+    if (prof) CK(capturing ? cudaEventRecordWithFlags(c->ev[k], s, cudaEventRecordExternal)
+                           : cudaEventRecord(c->ev[k], s));
+    return SKY_OK;
+  };
+  const uint64_t items = (uint64_t)sh.nv * sh.n;
+  launches = 0;
+  CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
+  CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
+  TRY(mark(0));
+  launch_preprocess(b, sh.n, sh.nv, s);
+  TRY(mark(1));
+  launch_scan(b, (uint32_t)items, s);
+  launch_group_bounds(b, s);
+  launches += 5;
+  if (sizing_sync) {
+    CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (c->h_st->total_isect > c->icap) {
+      TRY(ensure_isect(c, c->h_st->total_isect));
+      b = make_buffers(c);
+      c->h_sp->icap = c->icap;
+      CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
+      CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
+      launch_group_bounds(b, s);
+      ++launches;
+    }
+  }
+  TRY(mark(2));
+  launch_emit(b, sh.n, sh.nv, s);
+  TRY(mark(3));
+  DevStatus* dst = (DevStatus*)c->d_st.p;
+  for (uint32_t g = 0; g < sh.ngroups; ++g) {
+    SortSegment seg{&dst->group_bounds[g][0], 0};
+    CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap, sh.key_bits[g],
+                         c->sort, &dst->error, s));
+    launches += 2 + (sh.key_bits[g] + 7) / 8;
+  }
+  TRY(mark(4));
+  launch_ranges(b, c->icap, s);
+  TRY(mark(5));
+  launch_forward(b, sh.max_tiles, c->cfg.tile_size, sh.ssim, sh.nv, sh.max_view_px, s);
+  if (sh.with_loss) launch_loss_final(b, s);
+  launches += 4 + (sh.with_loss ? 1 : 0) + (sh.ssim ? 1 : 0);
+  TRY(mark(6));
+  if (sh.mode >= kBackward) {
+    if (sh.ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
+    launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.ref, s);
+    TRY(mark(7));
+    launch_geom_adam(b, sh.n, s);
+    launches += 2;
+  } else {
+    TRY(mark(7));
+  }
+  TRY(mark(8));
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
+  return SKY_OK;
+}
+
+void drop_graph(Context* c) {
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  c->gexec = nullptr;
+  c->gvalid = false;
+}
+
 // Runs one pass over `nv` cameras.  mode: render / forward (+loss) /
 // backward (gradients out, no Adam) / train (Adam step).
 int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepStats* stats) {
@@ -254,8 +348,21 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   const SkyConfig& cfg = c->cfg;
   const uint32_t ts = cfg.tile_size;
   const bool with_loss = mode != kRender;
+  // Training steps replay a captured graph once the intersection capacity is
+  // known (the first step runs directly and sizes it).
+  const bool graph = cfg.use_graph && mode == kTrain && c->icap > 0 && c->warm_steps > 0;
   StepParams& sp = *c->h_sp;
   memset(&sp, 0, sizeof(StepParams));
+  uint32_t max_cam_tiles = 0, max_cam_px = 0;
+  for (const SkyCamera& cam : c->cams) {
+    const uint64_t vt = (uint64_t)((cam.width + ts - 1) / ts) * ((cam.height + ts - 1) / ts);
+    if (vt > 65536)
+      return fail(SKY_ERR_ARG, "a camera has %llu tiles; at most 65536 per view", (unsigned long long)vt);
+    max_cam_tiles = std::max(max_cam_tiles, (uint32_t)vt);
+    max_cam_px = std::max(max_cam_px, cam.width * cam.height);
+  }
+  // graph mode: fixed slot -> sort group assignment
+  const uint32_t slots_per_group = std::max<uint32_t>(1, 65536 / std::max<uint32_t>(1, max_cam_tiles));
   // views, tiles, pixels, groups
   uint64_t tile_total = 0, pix_total = 0;
   uint32_t max_view_px = 0;
@@ -276,10 +383,8 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
     vi.tiles_x = (cam.width + ts - 1) / ts;
     vi.tiles_y = (cam.height + ts - 1) / ts;
     const uint64_t vt = (uint64_t)vi.tiles_x * vi.tiles_y;
-    if (vt > 65536)
-      return fail(SKY_ERR_ARG, "camera %u has %llu tiles; at most 65536 per view", ci,
-                  (unsigned long long)vt);
-    if (ngroups == 0 || group_tiles + vt > 65536) {
+    const bool new_group = graph ? (v % slots_per_group == 0) : (ngroups == 0 || group_tiles + vt > 65536);
+    if (new_group) {
       if (ngroups == (uint32_t)kMaxGroups) return fail(SKY_ERR_ARG, "too many sort groups");
       GroupInfo& g = sp.groups[ngroups];
       g.tile_begin = (uint32_t)tile_total;
@@ -300,10 +405,12 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
     pix_total += (uint64_t)cam.width * cam.height;
     g.tile_end = (uint32_t)tile_total;
     g.item_end = (v + 1) * c->n;
-    g.key_bits = 16 + ceil_log2((uint32_t)group_tiles);
+    g.key_bits = 16 + ceil_log2(graph ? slots_per_group * max_cam_tiles : (uint32_t)group_tiles);
     max_view_px = std::max(max_view_px, cam.width * cam.height);
   }
-  if (pix_total >= (1ull << 32)) return fail(SKY_ERR_ARG, "too many pixels in one step");
+  const uint64_t pix_cap = graph ? (uint64_t)nv * max_cam_px : pix_total;
+  const uint64_t tile_cap = graph ? (uint64_t)nv * max_cam_tiles : tile_total;
+  if (pix_cap >= (1ull << 32)) return fail(SKY_ERR_ARG, "too many pixels in one step");
   const uint64_t items = (uint64_t)nv * c->n;
   if (items >= (1ull << 32)) return fail(SKY_ERR_ARG, "views x Gaussians exceeds 2^32");
   // buffers
@@ -313,13 +420,13 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   TRY(dev_alloc(c, c->rects, items * 8));
   TRY(dev_alloc(c, c->cumsum, items * 4));
   TRY(dev_alloc(c, c->block_sums, (scan_block_count((uint32_t)items) + 1) * 4));
-  TRY(dev_alloc(c, c->offsets, (tile_total + 1) * 4));
-  TRY(dev_alloc(c, c->loss_partials, (tile_total + 1) * 8));
-  TRY(dev_alloc(c, c->color, pix_total * 16));
-  TRY(dev_alloc(c, c->alpha, pix_total * 4));
-  TRY(dev_alloc(c, c->tfinal, pix_total * 4));
-  TRY(dev_alloc(c, c->last, pix_total * 4));
-  TRY(dev_alloc(c, c->residual, pix_total * 16));
+  TRY(dev_alloc(c, c->offsets, (tile_cap + 1) * 4));
+  TRY(dev_alloc(c, c->loss_partials, (tile_cap + 1) * 8));
+  TRY(dev_alloc(c, c->color, pix_cap * 16));
+  TRY(dev_alloc(c, c->alpha, pix_cap * 4));
+  TRY(dev_alloc(c, c->tfinal, pix_cap * 4));
+  TRY(dev_alloc(c, c->last, pix_cap * 4));
+  TRY(dev_alloc(c, c->residual, pix_cap * 16));
   if (mode == kBackward) TRY(dev_alloc(c, c->grads, (size_t)kPlanes * c->stride * 4));
   const bool ref = cfg.backward_mode == SKY_BWD_REFERENCE;
   if (ref && mode >= kBackward) TRY(dev_alloc(c, c->gsum54, items * 54 * 8));
@@ -368,67 +475,61 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
     sp.bc1_rcp = (float)(1.0 / bc1);
     sp.bc2_sqrt_rcp = (float)(1.0 / std::sqrt(bc2));
   }
-  DevBuffers b = make_buffers(c);
+  Shape sh;
+  sh.nv = nv;
+  sh.n = c->n;
+  sh.stride = c->stride;
+  sh.mode = mode;
+  sh.max_tiles = (uint32_t)tile_cap;
+  sh.max_view_px = graph ? max_cam_px : max_view_px;
+  sh.ngroups = ngroups;
+  for (uint32_t g = 0; g < ngroups; ++g) sh.key_bits[g] = sp.groups[g].key_bits;
+  sh.with_loss = with_loss;
+  sh.ssim = with_loss && cfg.w_ssim > 0.0f;
+  sh.ref = ref;
+  sh.prof = c->profiling;
   cudaStream_t s = c->stream;
-  const bool prof = c->profiling;
-  auto mark = [&](int k) -> int {
-    if (prof) CK(cudaEventRecord(c->ev[k], s));
-    return SKY_OK;
-  };
   uint64_t launches = 0;
-  CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
-  CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
-  TRY(mark(0));
-  launch_preprocess(b, c->n, nv, s);
-  TRY(mark(1));
-  launch_scan(b, (uint32_t)items, s);
-  launch_group_bounds(b, s);
-  launches += 5;
-  // size the intersection buffers from the device count (the reference reads
-  // the projections back for its host cumsum at the same point)
-  CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  if (c->h_st->total_isect > c->icap) {
-    TRY(ensure_isect(c, c->h_st->total_isect));
-    b = make_buffers(c);
+  for (int attempt = 0;; ++attempt) {
+    sh.icap = c->icap;
     sp.icap = c->icap;
-    CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
-    CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
-    launch_group_bounds(b, s);
-    ++launches;
+    if (!graph) {
+      TRY(enqueue(c, sh, true, launches));
+    } else {
+      if (!c->gvalid || !c->gshape.same(sh)) {
+        drop_graph(c);
+        CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+        uint64_t l = 0;
+        int rc = enqueue(c, sh, false, l);
+        cudaGraph_t g = nullptr;
+        cudaError_t e = cudaStreamEndCapture(s, &g);
+        if (rc != SKY_OK) {
+          if (g) cudaGraphDestroy(g);
+          return rc;
+        }
+        if (e != cudaSuccess) return fail(SKY_ERR_CUDA, "graph capture: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&c->gexec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return fail(SKY_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(e));
+        c->gshape = sh;
+        c->gvalid = true;
+        c->graph_launches = l;
+        c->graph_captures += 1;
+      }
+      CK(cudaGraphLaunch(c->gexec, s));
+      launches = c->graph_launches;
+    }
+    CK(cudaStreamSynchronize(s));
+    c->launches += launches;
+    if (graph && (c->h_st->error & SKY_DEVERR_CAPACITY) && attempt < 3) {
+      // the failed replay changed no parameter: grow, re-capture, run again
+      TRY(ensure_isect(c, c->h_st->total_isect));
+      drop_graph(c);
+      continue;
+    }
+    break;
   }
-  TRY(mark(2));
-  launch_emit(b, c->n, nv, s);
-  TRY(mark(3));
-  DevStatus* dst = (DevStatus*)c->d_st.p;
-  for (uint32_t g = 0; g < ngroups; ++g) {
-    SortSegment seg{&dst->group_bounds[g][0], 0};
-    CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap,
-                         sp.groups[g].key_bits, c->sort, &dst->error, s));
-    launches += 2 + (sp.groups[g].key_bits + 7) / 8;
-  }
-  TRY(mark(4));
-  launch_ranges(b, c->icap, s);
-  TRY(mark(5));
-  launch_forward(b, (uint32_t)tile_total, ts, with_loss && cfg.w_ssim > 0.0f, nv, max_view_px, s);
-  if (with_loss) launch_loss_final(b, s);
-  launches += 4 + (with_loss ? 1 : 0) + (with_loss && cfg.w_ssim > 0.0f ? 1 : 0);
-  TRY(mark(6));
-  if (mode >= kBackward) {
-    if (ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
-    launch_backward(b, (uint32_t)tile_total, ts, ref, s);
-    TRY(mark(7));
-    launch_geom_adam(b, c->n, s);
-    launches += 2;
-  } else {
-    TRY(mark(7));
-  }
-  TRY(mark(8));
-  CK(cudaGetLastError());
-  CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
-  CK(cudaStreamSynchronize(s));
-  c->launches += launches;
-  if (prof) {
+  if (sh.prof) {
     for (int k = 0; k < SKY_NUM_STAGES; ++k) {
       float ms = 0.0f;
       CK(cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]));
@@ -452,6 +553,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   if (mode == kTrain) {
     c->iteration = it;
     c->adam_steps += 1;
+    c->warm_steps += 1;
   }
   if (stats) {
     stats->iteration = c->iteration;
@@ -560,6 +662,7 @@ int sky_destroy(void* p) {
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
                 &c->flag_scan, &c->d_sp, &c->d_st};
   for (Buf* b : all) dev_free(c, *b);
+  drop_graph(c);
   for (int k = 0; k <= SKY_NUM_STAGES; ++k)
     if (c->ev[k]) cudaEventDestroy(c->ev[k]);
   if (c->h_sp) cudaFreeHost(c->h_sp);

@@ -1,0 +1,54 @@
+"""The captured-graph training step (use_graph) gives bit-identical
+parameters to direct launches, also when a step overflows the intersection
+capacity the graph was captured with (grow, re-capture, run again)."""
+import numpy as np
+import pytest
+
+from skyfall import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def trainer(sky, P, cams, tgt, graph):
+    r = sky.GaussianRenderer(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0,
+                             use_graph=int(graph), sh_update_interval=2)
+    r.load_points(P)
+    r.setTrainingCameras(cams)
+    r.setTrainingImages(tgt)
+    return r
+
+
+def test_graph_replay_matches_direct_launches(sky):
+    P = scenes.scene_clusters(30000, seed=51, clusters=8, center_range=1.0, logscale_mean=-4.0)
+    cams = scenes.cameras_mixed(6, 4.0, seed=52)
+    cams = [dict(c, width=c["width"] // 4, height=c["height"] // 4,
+                 focal=c["focal"] / 4, proj=c["proj"]) for c in cams]
+    tgt = [scenes.target_uniform(c["width"], c["height"], seed=60 + k) for k, c in enumerate(cams)]
+    plan = [[0, 1, 2], [3, 4, 5], [5, 0, 3], [1, 1, 2], [4, 2, 0]]
+    out = []
+    for graph in (False, True):
+        r = trainer(sky, P, cams, tgt, graph)
+        losses = [r.trainStep(v).loss for v in plan]
+        out.append((losses, r.params(), r.moments()))
+        r.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2][0], out[1][2][0]) and np.array_equal(out[0][2][1], out[1][2][1])
+
+
+def test_graph_regrows_capacity(sky):
+    P = scenes.scene_clusters(40000, seed=53, clusters=8, center_range=1.0, logscale_mean=-4.0)
+    far = scenes.camera_fov((0.0, 0.5, 9.0), 160, 120)
+    near = scenes.camera_fov((0.0, 0.2, 2.2), 160, 120)
+    cams = [far, near]
+    tgt = [scenes.target_uniform(160, 120, seed=70 + k) for k in range(2)]
+    plan = [[0], [0], [1], [1, 0]]     # the near view has many more intersections
+    out = []
+    for graph in (False, True):
+        r = trainer(sky, P, cams, tgt, graph)
+        isects = [r.trainStep(v).num_intersections for v in plan]
+        out.append((isects, r.params()))
+        r.close()
+    assert out[0][0][2] > 2 * out[0][0][0]
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])

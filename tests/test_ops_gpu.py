@@ -108,9 +108,9 @@ def test_load_packed_reference_layout(sky):
     h[:, 4] = P[9]               # rot0 = w
     h[:, 5:8] = P[6:9].T         # rot1..rot3 = x, y, z
     h[:, 8:11] = P[3:6].T
-    sh = P[11:59].T.astype(np.float16)
+    sh = np.ascontiguousarray(P[11:59].T.astype(np.float16))
     r = sky.GaussianRenderer(sh_degree=3)
-    r.load_packed(h.view(np.uint32), sh.view(np.uint32))
+    r.load_packed(np.ascontiguousarray(h).view(np.uint32), sh.view(np.uint32))
     assert np.array_equal(r.params(), P)
 
 
