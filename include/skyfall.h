@@ -127,6 +127,8 @@ typedef struct SkyStatus {
   uint32_t num_cameras;
   uint32_t error_flags;       /* sticky device error word (0 = none)        */
   uint64_t kernel_launches;   /* kernels launched by the context so far     */
+  uint64_t graph_replays;     /* training steps run as a graph replay       */
+  uint64_t graph_captures;    /* graph (re-)captures                        */
 } SkyStatus;
 
 /* Stages timed by sky_set_profiling / sky_get_stage_times, in order.  The

@@ -151,7 +151,7 @@ struct Context {
   cudaGraphExec_t gexec = nullptr;
   Shape gshape;
   bool gvalid = false;
-  uint64_t graph_launches = 0, graph_captures = 0, warm_steps = 0;
+  uint64_t graph_launches = 0, graph_captures = 0, graph_replays = 0, warm_steps = 0;
 };
 
 int dev_alloc(Context* c, Buf& b, size_t bytes, bool keep = false) {
@@ -518,6 +518,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
       }
       CK(cudaGraphLaunch(c->gexec, s));
       launches = c->graph_launches;
+      c->graph_replays += 1;
     }
     CK(cudaStreamSynchronize(s));
     c->launches += launches;
@@ -922,6 +923,8 @@ int sky_get_status(void* p, SkyStatus* st) {
   st->num_cameras = (uint32_t)c->cams.size();
   st->error_flags = c->error_flags;
   st->kernel_launches = c->launches;
+  st->graph_replays = c->graph_replays;
+  st->graph_captures = c->graph_captures;
   return SKY_OK;
 }
 

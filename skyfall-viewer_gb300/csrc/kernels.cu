@@ -630,42 +630,50 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
           const float al = op * G;
           const float a = fmin_(al, MAX_ALPHA);
           if (a >= MIN_ALPHA) {
+            // The decision above repeats the forward's bit for bit; the
+            // gradient arithmetic below only has to be accurate, so it uses
+            // fused multiply-adds and the fast reciprocal division.
             contrib = true;
             const float cr = q1.z, cg = q1.w, cbl = q2.x;
             const float om = fmax_(1.0f - a, 0.0001f);
-            const float Tb = T / om;
+            const float Tb = __fdividef(T, om);
             const float ctb = a * Tb;
-            float fg = r0 * cr + r1 * cg;
-            fg = fg + r2 * cbl;
-            float bgt = r0 * acc0 + r1 * acc1;
-            bgt = bgt + r2 * acc2;
+            const float fg = __fmaf_rn(r2, cbl, __fmaf_rn(r1, cg, r0 * cr));
+            const float bgt = __fmaf_rn(r2, acc2, __fmaf_rn(r1, acc1, r0 * acc0));
             const float dLda = (fg - bgt) * Tb;
-            float dlogit = (dLda * a) * (1.0f - op);
-            float dLdG = dLda * op;
-            if (al > MAX_ALPHA) {
-              dlogit = 0.0f;
-              dLdG = 0.0f;
-            }
-            const float dLds = dLdG * (-G);
+            const bool live = !(al > MAX_ALPHA);  // the alpha clamp has zero slope
+            const float dlogit = live ? (dLda * a) * (1.0f - op) : 0.0f;
+            const float dLds = live ? -(dLda * op) * G : 0.0f;
+            const float hds = 0.5f * dLds;
             val[0] = r0 * ctb;
             val[1] = r1 * ctb;
             val[2] = r2 * ctb;
             val[3] = dlogit;
-            val[4] = ((dLds * 0.5f) * dx) * dx;
+            val[4] = (hds * dx) * dx;
             val[5] = (dLds * dx) * dy;
-            val[6] = ((dLds * 0.5f) * dy) * dy;
-            val[7] = -(dLds * ((q0.z * dx) + (q0.w * dy)));
-            val[8] = -(dLds * ((q0.w * dx) + (q1.x * dy)));
-            acc0 = a * cr + (1.0f - a) * acc0;
-            acc1 = a * cg + (1.0f - a) * acc1;
-            acc2 = a * cbl + (1.0f - a) * acc2;
+            val[6] = (hds * dy) * dy;
+            val[7] = -dLds * __fmaf_rn(q0.z, dx, q0.w * dy);
+            val[8] = -dLds * __fmaf_rn(q0.w, dx, q1.x * dy);
+            acc0 = __fmaf_rn(a, cr - acc0, acc0);
+            acc1 = __fmaf_rn(a, cg - acc1, acc1);
+            acc2 = __fmaf_rn(a, cbl - acc2, acc2);
             T = Tb;
           }
         }
       }
-      float tot = 0.0f;
-      if (__any_sync(kFull, contrib)) tot = warp_reduce_scatter9(val, lane);
-      if (slot < 9) s_part[warp][j][slot] = tot;
+      const uint32_t who = __ballot_sync(kFull, contrib);
+      if (who == 0u) {
+        if (slot < 9) s_part[warp][j][slot] = 0.0f;
+      } else if ((who & (who - 1u)) == 0u) {
+        // a single contributing pixel: its values are the warp's sums
+        if (contrib) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) s_part[warp][j][k] = val[k];
+        }
+      } else {
+        const float tot = warp_reduce_scatter9(val, lane);
+        if (slot < 9) s_part[warp][j][slot] = tot;
+      }
     }
     __syncthreads();
     for (int j = (int)tid; j < cnt; j += NT) {

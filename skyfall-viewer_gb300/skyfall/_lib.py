@@ -86,7 +86,8 @@ class SkyStatus(C.Structure):
     _fields_ = [("iteration", C.c_uint64), ("adam_steps", C.c_uint64),
                 ("last_intersections", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("num_gaussians", C.c_uint32), ("capacity", C.c_uint32), ("num_cameras", C.c_uint32),
-                ("error_flags", C.c_uint32), ("kernel_launches", C.c_uint64)]
+                ("error_flags", C.c_uint32), ("kernel_launches", C.c_uint64),
+                ("graph_replays", C.c_uint64), ("graph_captures", C.c_uint64)]
 
 
 STAGES = ["preprocess", "scan", "emit", "sort", "ranges", "forward", "backward", "geom_adam"]

@@ -38,17 +38,20 @@ def test_graph_replay_matches_direct_launches(sky):
 
 def test_graph_regrows_capacity(sky):
     P = scenes.scene_clusters(40000, seed=53, clusters=8, center_range=1.0, logscale_mean=-4.0)
-    far = scenes.camera_fov((0.0, 0.5, 9.0), 160, 120)
-    near = scenes.camera_fov((0.0, 0.2, 2.2), 160, 120)
+    far = scenes.camera_fov((0.0, 0.5, 14.0), 160, 120)
+    near = scenes.camera_fov((0.0, 0.2, 2.5), 800, 600)
     cams = [far, near]
-    tgt = [scenes.target_uniform(160, 120, seed=70 + k) for k in range(2)]
+    tgt = [scenes.target_uniform(c["width"], c["height"], seed=70 + k) for k, c in enumerate(cams)]
     plan = [[0], [0], [1], [1, 0]]     # the near view has many more intersections
     out = []
     for graph in (False, True):
         r = trainer(sky, P, cams, tgt, graph)
         isects = [r.trainStep(v).num_intersections for v in plan]
-        out.append((isects, r.params()))
+        st = r.getStatus()
+        out.append((isects, r.params(), st.graph_replays, st.graph_captures))
         r.close()
-    assert out[0][0][2] > 2 * out[0][0][0]
+    assert out[0][0][2] > 2 * out[0][0][0]     # beyond the 1.5x headroom of step 1
     assert out[0][0] == out[1][0]
     assert np.array_equal(out[0][1], out[1][1])
+    assert out[0][2] == 0 and out[1][2] >= 3   # steps 2.. replayed a graph
+    assert out[1][3] >= 2                      # and it was re-captured after growing
