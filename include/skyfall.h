@@ -264,6 +264,20 @@ int sky_get_stage_times(void* ctx, double* ms, uint32_t n, uint64_t* steps);
 int sky_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                    uint32_t* vals_out, uint32_t n, uint32_t key_bits, void* stream);
 
+/* The same sort for callers that cannot let the library allocate device
+ * memory (a host that owns the whole GPU through its own pool or caching
+ * allocator, or code that must not call cudaMalloc mid-work).  It has no
+ * counterpart in the reference.  It allocates nothing: its scratch is one
+ * fixed device array (about 9 MiB, held by every GPU that loads the library
+ * until the process exits), so n is limited to SKY_SORT_NOALLOC_MAX_KEYS
+ * (larger n returns SKY_ERR_ARG).  The first call on a device looks up that
+ * array's address with the device current; make it before any stream
+ * capture begins.  All calls share the array: calls whose GPU work overlaps
+ * race with each other and must be serialised.                             */
+#define SKY_SORT_NOALLOC_MAX_KEYS (1u << 20)
+int sky_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
+                           uint32_t* vals_out, uint32_t n, uint32_t key_bits, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1161,3 +1161,12 @@ extern "C" int sky_reset_opacity(void* p, float max_opacity) {
   CK(cudaStreamSynchronize(c->stream));
   return SKY_OK;
 }
+
+namespace sky {
+// Sets the calling thread's sky_last_error() message; returns `code`.  Lets
+// entry points defined in other translation units report errors.
+int record_error(int code, const char* msg) {
+  g_err = msg;
+  return code;
+}
+}  // namespace sky

@@ -140,6 +140,7 @@ PROTOTYPES = {
     "sky_read_buffer": (I32, [P, I32, P, U64, C.POINTER(U64)]),
     "sky_sync": (I32, [P]),
     "sky_sort_pairs": (I32, [P, P, P, P, U32, U32, P]),
+    "sky_sort_pairs_noalloc": (I32, [P, P, P, P, U32, U32, P]),
     "sky_get_stream": (I32, [P, C.POINTER(C.c_void_p)]),
     "sky_set_profiling": (I32, [P, I32]),
     "sky_get_stage_times": (I32, [P, C.POINTER(C.c_double), U32, C.POINTER(U64)]),
