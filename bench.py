@@ -272,6 +272,7 @@ def main():
     e2e_value = args.steps * B / res["wall"] * world
 
     plain = None
+    plain_stage_ms = None
     if not args.no_plain:
         # the plain per-view path: one view and one Adam step per sky_step,
         # launched directly with the host-side sizing read-back
@@ -282,6 +283,7 @@ def main():
             r.trainStep([k % C])
         pr = time_steps(r, torch, psets, 0)
         plain = len(psets) / (pr["ms"] / 1000.0)
+        plain_stage_ms = {k: v / max(pr["steps"], 1) for k, v in pr["stages"].items()}
 
     # roofline of the dominant stage
     steps = max(res["steps"], 1)
@@ -335,6 +337,7 @@ def main():
         },
         "mpix_per_s": mpix,
         "plain_iters_per_s": plain,
+        "plain_stage_ms": plain_stage_ms,
         "batched_over_plain": (value / world / plain) if plain else None,
         "stage_ms": stage_ms,
         "intersections_per_step": isect,

@@ -35,21 +35,8 @@ SKY_DEV bool capacity_failed(const DevStatus* st) {
   return *(volatile const uint32_t*)&st->error != 0u;
 }
 
-// ---------------------------------------------------------------------------
-// Preprocess: one thread per (view, Gaussian) item.  Grid (ceil(N/256), V).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_preprocess(DevBuffers b) {
-  const StepParams& sp = *b.sp;
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t v = blockIdx.y;
-  if (g >= sp.n || v >= sp.num_views) return;
-  const ViewInfo& vi = sp.views[v];
-  const bool r16 = sp.round_f16 != 0;
-  const uint32_t stride = sp.plane_stride;
-  auto get = [&](int plane) { return load_plane(b.params, stride, plane, g, r16); };
-  ProjOut o;
-  const bool ok = project_gaussian(get, vi, sp, (int)sp.sh_deg, true, o);
-  const size_t item = (size_t)v * sp.n + g;
+// Writes the raster record, depth/radius, tile count and rectangle of one item.
+SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, size_t item) {
   // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
   // whatever the rounding of exp (|error| < 1e-6 << 1e-3), so skipping it
   // there decides as the reference does.  The pixels with s <= smax lie in
@@ -74,6 +61,32 @@ __global__ void __launch_bounds__(256) k_preprocess(DevBuffers b) {
   b.aux[item] = make_float2(o.depth, o.radius);
   b.counts[item] = o.count;
   b.rects[item] = make_uint2(o.x0 | (o.y0 << 16), o.x1 | (o.y1 << 16));
+}
+
+// ---------------------------------------------------------------------------
+// Preprocess: one thread per Gaussian; its parameters are read (and rounded
+// to f16) once and projected into every view of the step.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_preprocess(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= sp.n) return;
+  const bool r16 = sp.round_f16 != 0;
+  const uint32_t stride = sp.plane_stride;
+  const int deg = (int)sp.sh_deg;
+  const int nsh = 3 * (deg + 1) * (deg + 1);
+  float prm[kPlanes];
+#pragma unroll
+  for (int k = 0; k < kPlanes; ++k)
+    prm[k] = (k < 11 + nsh) ? load_plane(b.params, stride, k, g, r16) : 0.0f;
+  auto get = [&](int plane) { return prm[plane]; };
+  for (uint32_t v = 0; v < sp.num_views; ++v) {
+    const ViewInfo& vi = sp.views[v];
+    ProjOut o;
+    const bool ok = project_gaussian(get, vi, sp, deg, true, o);
+    const size_t item = (size_t)v * sp.n + g;
+    write_projection(b, o, ok, item);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -207,31 +220,33 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
 // gaussian-renderer.ts:1966-2020).  Also resolves the item of every sorted
 // intersection.
 // ---------------------------------------------------------------------------
+// Grid-stride over the step's intersections: the grid is sized for the
+// capacity's order of magnitude, not the capacity itself.
 __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
   const StepParams& sp = *b.sp;
   if (capacity_failed(b.status)) return;
-  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t total = min(b.status->total_isect, sp.icap);
-  if (i >= total) return;
-  int g = 0;
-  for (int k = 0; k < (int)sp.num_groups; ++k)
-    if (b.status->group_bounds[k][0] <= i && i < b.status->group_bounds[k][1]) g = k;
-  const GroupInfo& gi = sp.groups[g];
-  const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
-  const uint32_t t = gi.tile_begin + (b.keys_sorted[i] >> 16);
-  if (t >= gi.tile_end || (i > gb && gi.tile_begin + (b.keys_sorted[i - 1] >> 16) > t)) {
-    atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);  // unsorted or corrupt keys
-    return;
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    int g = 0;
+    for (int k = 0; k < (int)sp.num_groups; ++k)
+      if (b.status->group_bounds[k][0] <= i && i < b.status->group_bounds[k][1]) g = k;
+    const GroupInfo& gi = sp.groups[g];
+    const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
+    const uint32_t t = gi.tile_begin + (b.keys_sorted[i] >> 16);
+    if (t >= gi.tile_end || (i > gb && gi.tile_begin + (b.keys_sorted[i - 1] >> 16) > t)) {
+      atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);  // unsorted or corrupt keys
+      return;
+    }
+    if (i == gb) {
+      for (uint32_t u = gi.tile_begin; u <= t; ++u) b.offsets[u] = i;
+    } else {
+      const uint32_t tp = gi.tile_begin + (b.keys_sorted[i - 1] >> 16);
+      for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
+    }
+    if (i + 1 == ge)
+      for (uint32_t u = t + 1; u < gi.tile_end; ++u) b.offsets[u] = ge;
+    b.flatten[i] = b.rec_of[b.vals_sorted[i]];
   }
-  if (i == gb) {
-    for (uint32_t u = gi.tile_begin; u <= t; ++u) b.offsets[u] = i;
-  } else {
-    const uint32_t tp = gi.tile_begin + (b.keys_sorted[i - 1] >> 16);
-    for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
-  }
-  if (i + 1 == ge)
-    for (uint32_t u = t + 1; u < gi.tile_end; ++u) b.offsets[u] = ge;
-  b.flatten[i] = b.rec_of[b.vals_sorted[i]];
 }
 
 // Empty groups and the final sentinel offsets[num_tiles] = total.
@@ -865,8 +880,8 @@ struct Grad11 {
 
 SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& sp,
                         const float* prm /*11 geometry params*/, const float in9[9],
-                        bool color_dir, const float* sh /*48, may be null*/, int deg,
-                        Grad11& gr) {
+                        bool color_dir, const float* sh /*48 values at sh[k * sh_stride]*/,
+                        int sh_stride, int deg, Grad11& gr) {
   // mean -> camera space
   float dpc[3] = {0.f, 0.f, 0.f};
   float clip[4];
@@ -975,7 +990,8 @@ SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& 
     for (int c = 0; c < 3; ++c) draw[c] = o.raw[c] > 0.0f ? in9[c] : 0.0f;
     float ddir[3] = {0.f, 0.f, 0.f};
     auto addk = [&](int k, float gx, float gy, float gz) {
-      float s = draw[0] * sh[3 * k] + draw[1] * sh[3 * k + 1] + draw[2] * sh[3 * k + 2];
+      float s = draw[0] * sh[(3 * k) * sh_stride] + draw[1] * sh[(3 * k + 1) * sh_stride] +
+                draw[2] * sh[(3 * k + 2) * sh_stride];
       ddir[0] += s * gx;
       ddir[1] += s * gy;
       ddir[2] += s * gz;
@@ -1026,10 +1042,18 @@ SKY_DEV void adam_elem(float* __restrict__ p, float* __restrict__ m1, float* __r
   m2[idx] = nm2;
 }
 
-__global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
+constexpr int kGeomThreads = 128;
+
+// SH values and SH-gradient accumulators live in shared memory (one column
+// per thread, conflict-free), which keeps the kernel under 128 registers and
+// four blocks per multiprocessor resident.
+__global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
+  __shared__ float s_sh[48][kGeomThreads];
+  __shared__ float s_gsh[48][kGeomThreads];
   const StepParams& sp = *b.sp;
   if (capacity_failed(b.status)) return;
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x;
+  const uint32_t g = blockIdx.x * blockDim.x + t;
   if (g >= sp.n) return;
   const uint32_t stride = sp.plane_stride;
   const bool r16 = sp.round_f16 != 0;
@@ -1040,22 +1064,17 @@ __global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
   float prm[11];
 #pragma unroll
   for (int k = 0; k < 11; ++k) prm[k] = load_plane_rw(b.params, stride, k, g, r16);
-  float sh[48];
-#pragma unroll
-  for (int k = 0; k < 48; ++k)
-    sh[k] = (!ref && k < 3 * ncoef) ? load_plane_rw(b.params, stride, 11 + k, g, r16) : 0.0f;
+  for (int k = 0; k < 48; ++k) {
+    s_sh[k][t] = (!ref && k < 3 * ncoef) ? load_plane_rw(b.params, stride, 11 + k, g, r16) : 0.0f;
+    s_gsh[k][t] = 0.0f;
+  }
   Grad11 gr;
 #pragma unroll
   for (int k = 0; k < 3; ++k) { gr.pos[k] = 0.f; gr.ls[k] = 0.f; }
 #pragma unroll
   for (int k = 0; k < 4; ++k) gr.q[k] = 0.f;
   gr.logit = 0.f;
-  float gsh[48];
-#pragma unroll
-  for (int k = 0; k < 48; ++k) gsh[k] = 0.0f;
-  auto get = [&](int plane) {
-    return plane < 11 ? prm[plane] : (plane - 11 < 48 ? sh[plane - 11] : 0.0f);
-  };
+  auto get = [&](int plane) { return plane < 11 ? prm[plane] : s_sh[plane - 11][t]; };
   for (uint32_t v = 0; v < sp.num_views; ++v) {
     const size_t item = (size_t)v * sp.n + g;
     const uint32_t cnt = b.counts[item];
@@ -1063,10 +1082,24 @@ __global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
     float in9[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
-    float shref[48];
+    bool any = false;
     if (!ref) {
       const uint32_t e1 = b.cumsum[item], e0 = e1 - cnt;
-      for (uint32_t e = e0; e < e1; ++e) {
+      uint32_t e = e0;
+      for (; e + 1 < e1; e += 2) {  // two partials in flight
+        const float4 a0 = b.partials[(size_t)e * 3 + 0];
+        const float4 a1 = b.partials[(size_t)e * 3 + 1];
+        const float4 a2 = b.partials[(size_t)e * 3 + 2];
+        const float4 c0 = b.partials[(size_t)e * 3 + 3];
+        const float4 c1 = b.partials[(size_t)e * 3 + 4];
+        const float4 c2 = b.partials[(size_t)e * 3 + 5];
+        in9[0] = (in9[0] + a0.x) + c0.x; in9[1] = (in9[1] + a0.y) + c0.y;
+        in9[2] = (in9[2] + a0.z) + c0.z; in9[3] = (in9[3] + a0.w) + c0.w;
+        in9[4] = (in9[4] + a1.x) + c1.x; in9[5] = (in9[5] + a1.y) + c1.y;
+        in9[6] = (in9[6] + a1.z) + c1.z; in9[7] = (in9[7] + a1.w) + c1.w;
+        in9[8] = (in9[8] + a2.x) + c2.x;
+      }
+      if (e < e1) {
         const float4 a0 = b.partials[(size_t)e * 3 + 0];
         const float4 a1 = b.partials[(size_t)e * 3 + 1];
         const float4 a2 = b.partials[(size_t)e * 3 + 2];
@@ -1074,41 +1107,36 @@ __global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
         in9[3] = in9[3] + a0.w; in9[4] = in9[4] + a1.x; in9[5] = in9[5] + a1.y;
         in9[6] = in9[6] + a1.z; in9[7] = in9[7] + a1.w; in9[8] = in9[8] + a2.x;
       }
+#pragma unroll
+      for (int k = 0; k < 9; ++k) any = any || in9[k] != 0.0f;
     } else {
-      const long long* s = b.gsum54 + item * 54;
+      const long long* sref = b.gsum54 + item * 54;
       const float sc = 1.0f / 65536.0f;
-      in9[3] = (float)s[0] * sc;
-      in9[4] = (float)s[1] * sc; in9[5] = (float)s[2] * sc; in9[6] = (float)s[3] * sc;
-      in9[7] = (float)s[4] * sc; in9[8] = (float)s[5] * sc;
+      in9[3] = (float)sref[0] * sc;
+      in9[4] = (float)sref[1] * sc; in9[5] = (float)sref[2] * sc; in9[6] = (float)sref[3] * sc;
+      in9[7] = (float)sref[4] * sc; in9[8] = (float)sref[5] * sc;
 #pragma unroll
-      for (int k = 0; k < 48; ++k) shref[k] = (float)s[6 + k] * sc;
-    }
-    bool any = false;
-#pragma unroll
-    for (int k = 0; k < 9; ++k) any = any || in9[k] != 0.0f;
-    if (ref) {
-#pragma unroll
-      for (int k = 0; k < 48; ++k) any = any || shref[k] != 0.0f;
+      for (int k = 0; k < 9; ++k) any = any || in9[k] != 0.0f;
+      for (int k = 0; k < 48; ++k) {
+        const long long q = sref[6 + k];
+        any = any || q != 0;
+        if (need_sh_grads) s_gsh[k][t] += (float)q * sc;
+      }
     }
     if (!any) continue;
     const ViewInfo& vi = sp.views[v];
     ProjOut o;
     if (!project_gaussian(get, vi, sp, deg, !ref, o)) continue;
-    geom_chain(o, vi, sp, prm, in9, !ref, sh, deg, gr);
-    if (need_sh_grads) {
-      if (!ref) {
-        float Y[16];
-        sh_basis(o.dir[0], o.dir[1], o.dir[2], deg, Y);
+    geom_chain(o, vi, sp, prm, in9, !ref, &s_sh[0][t], kGeomThreads, deg, gr);
+    if (need_sh_grads && !ref) {
+      float Y[16];
+      sh_basis(o.dir[0], o.dir[1], o.dir[2], deg, Y);
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          const float dr = o.raw[c] > 0.0f ? in9[c] : 0.0f;
+      for (int c = 0; c < 3; ++c) {
+        const float dr = o.raw[c] > 0.0f ? in9[c] : 0.0f;
 #pragma unroll
-          for (int k = 0; k < 16; ++k)
-            if (k < ncoef) gsh[3 * k + c] += Y[k] * dr;
-        }
-      } else {
-#pragma unroll
-        for (int k = 0; k < 48; ++k) gsh[k] += shref[k];
+        for (int k = 0; k < 16; ++k)
+          if (k < ncoef) s_gsh[3 * k + c][t] += Y[k] * dr;
       }
     }
   }
@@ -1117,8 +1145,7 @@ __global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
   if (sp.write_grads) {
 #pragma unroll
     for (int k = 0; k < 11; ++k) b.grads[(size_t)k * stride + g] = g11[k];
-#pragma unroll
-    for (int k = 0; k < 48; ++k) b.grads[(size_t)(11 + k) * stride + g] = gsh[k];
+    for (int k = 0; k < 48; ++k) b.grads[(size_t)(11 + k) * stride + g] = s_gsh[k][t];
   }
   if (sp.apply_adam) {
 #pragma unroll
@@ -1127,9 +1154,8 @@ __global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
       adam_elem(b.params, b.m1, b.m2, (size_t)k * stride + g, g11[k], lr, sp);
     }
     if (sp.sh_update) {
-#pragma unroll
       for (int k = 0; k < 48; ++k)
-        adam_elem(b.params, b.m1, b.m2, (size_t)(11 + k) * stride + g, gsh[k], sp.lr_sh, sp);
+        adam_elem(b.params, b.m1, b.m2, (size_t)(11 + k) * stride + g, s_gsh[k][t], sp.lr_sh, sp);
     }
   }
 }
@@ -1140,8 +1166,8 @@ __global__ void __launch_bounds__(128) k_geom_adam(DevBuffers b) {
 // Launchers
 // ---------------------------------------------------------------------------
 void launch_preprocess(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s) {
-  dim3 grid((n + 255) / 256, views);
-  k_preprocess<<<grid, 256, 0, s>>>(b);
+  (void)views;
+  k_preprocess<<<(n + 255) / 256, 256, 0, s>>>(b);
 }
 
 void launch_scan(const DevBuffers& b, uint32_t n_items, cudaStream_t s) {
@@ -1162,7 +1188,10 @@ void launch_emit(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s
 }
 
 void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s) {
-  if (icap) k_ranges<<<(icap + 255) / 256, 256, 0, s>>>(b);
+  if (icap) {
+    const uint32_t blocks = min((icap + 255) / 256, (uint32_t)sm_count() * 16);
+    k_ranges<<<blocks, 256, 0, s>>>(b);
+  }
   k_ranges_empty<<<1, 256, 0, s>>>(b);
 }
 
@@ -1201,7 +1230,7 @@ void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool 
 
 void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s) {
   if (n == 0) return;
-  k_geom_adam<<<(n + 127) / 128, 128, 0, s>>>(b);
+  k_geom_adam<<<(n + kGeomThreads - 1) / kGeomThreads, kGeomThreads, 0, s>>>(b);
 }
 
 }  // namespace sky

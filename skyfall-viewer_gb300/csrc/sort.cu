@@ -83,11 +83,18 @@ k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, uint
   }
 }
 
-// Exclusive scan of each pass's 256 digit counts (one block per pass).
-__global__ void __launch_bounds__(kRadix) k_sort_scan(uint32_t* __restrict__ hist) {
+// Exclusive scan of each pass's 256 digit counts (one block per pass), and
+// trivial[pass] = 1 when one digit holds every key (the pass would be the
+// identity permutation, e.g. the high byte of the integer depth).
+__global__ void __launch_bounds__(kRadix)
+k_sort_scan(uint32_t* __restrict__ hist, SortSegment seg, uint32_t* __restrict__ trivial) {
   __shared__ uint32_t s_warp[kRadix / 32];
+  uint32_t begin, n;
+  seg_bounds(seg, begin, n);
   uint32_t* h = hist + blockIdx.x * kRadix;
   uint32_t v = h[threadIdx.x];
+  const int one_digit = __syncthreads_or(v == n);
+  if (threadIdx.x == 0) trivial[blockIdx.x] = one_digit ? 1u : 0u;
   uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
 #pragma unroll
@@ -103,10 +110,10 @@ __global__ void __launch_bounds__(kRadix) k_sort_scan(uint32_t* __restrict__ his
 }
 
 __global__ void __launch_bounds__(kSortThreads)
-k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
-           uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, SortSegment seg,
-           int pass, uint32_t key_bits, const uint32_t* __restrict__ hist,
-           uint32_t* __restrict__ tile_counter,
+k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_dst_out,
+           uint32_t* vals_dst_out, uint32_t* keys_tmp, uint32_t* vals_tmp, SortSegment seg,
+           int pass, int passes, const uint32_t* __restrict__ trivial, uint32_t key_bits,
+           const uint32_t* __restrict__ hist, uint32_t* __restrict__ tile_counter,
            uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_keys[kSortTile];
   __shared__ uint32_t s_vals[kSortTile];
@@ -116,9 +123,42 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
   __shared__ uint32_t s_scan[kWarps];
   __shared__ uint32_t s_tile;
 
+  // Trivial passes are skipped; the m remaining passes alternate between the
+  // temporary and the output buffers so that the last one writes the output
+  // (with m == 0, pass 0 runs anyway and copies).
+  int m = 0, j = 0;
+  bool skip = false;
+  for (int p = 0; p < passes; ++p) {
+    const bool t = trivial[p] != 0u;
+    if (!t) {
+      if (p < pass) ++j;
+      ++m;
+    }
+    if (p == pass) skip = t;
+  }
+  if (m == 0) {
+    if (pass != 0) return;
+    skip = false;
+    m = 1;
+  }
+  if (skip) return;
+  auto buf_of = [&](int jj, bool key) -> uint32_t* {
+    const bool to_out = ((m - 1 - jj) % 2) == 0;
+    return key ? (to_out ? keys_dst_out : keys_tmp) : (to_out ? vals_dst_out : vals_tmp);
+  };
+  const uint32_t* __restrict__ keys_in = j == 0 ? keys_src : buf_of(j - 1, true);
+  const uint32_t* __restrict__ vals_in = j == 0 ? vals_src : buf_of(j - 1, false);
+  uint32_t* __restrict__ keys_out = buf_of(j, true);
+  uint32_t* __restrict__ vals_out = buf_of(j, false);
+
   uint32_t begin, n;
   seg_bounds(seg, begin, n);
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // Persistent: each block takes tile tickets in order until the segment is
+  // done.  A block only waits (look-back) on lower tickets, which were handed
+  // to blocks already running, so any grid size makes progress.
+  for (;;) {
+  __syncthreads();  // the previous tile's shared-memory reads are complete
   if (tid == 0) s_tile = atomicAdd(&tile_counter[pass], 1u);
   for (int i = tid; i < kWarps * kRadix; i += kSortThreads) (&s_warp_hist[0][0])[i] = 0u;
   __syncthreads();
@@ -229,9 +269,22 @@ k_onesweep(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ va
     keys_out[begin + gp] = kk;
     vals_out[begin + gp] = s_vals[i];
   }
+  }  // next tile
 }
 
 }  // namespace
+
+int sm_count() {
+  static int cache[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!cache[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 132;
+  }
+  return cache[dev];
+}
 
 size_t sort_scratch_bytes(uint32_t max_n) {
   uint32_t tiles = (max_n + kSortTile - 1) / kSortTile + 1;
@@ -277,19 +330,14 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
   uint32_t hist_blocks = tiles < 1024u ? tiles : 1024u;
   k_sort_hist<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, seg, passes, key_bits, sc.hist,
                                                          sc.lookback, sc.max_tiles);
-  k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist);
-  const uint32_t* src_k = keys_in;
-  const uint32_t* src_v = vals_in;
-  for (int p = 0; p < passes; ++p) {
-    bool to_out = ((passes - 1 - p) % 2) == 0;
-    uint32_t* dk = to_out ? keys_out : sc.keys_tmp;
-    uint32_t* dv = to_out ? vals_out : sc.vals_tmp;
-    k_onesweep<<<tiles, kSortThreads, 0, stream>>>(src_k, src_v, dk, dv, seg, p, key_bits, sc.hist,
-                                                    sc.tile_counter, sc.lookback, sc.max_tiles,
-                                                    err);
-    src_k = dk;
-    src_v = dv;
-  }
+  uint32_t* trivial = sc.tile_counter + 8;  // cleared with the tile tickets above
+  k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist, seg, trivial);
+  for (int p = 0; p < passes; ++p)
+    k_onesweep<<<std::min<uint32_t>(tiles, (uint32_t)sm_count() * 4), kSortThreads, 0,
+                 stream>>>(keys_in, vals_in, keys_out, vals_out,
+                                                    sc.keys_tmp, sc.vals_tmp, seg, p, passes,
+                                                    trivial, key_bits, sc.hist, sc.tile_counter,
+                                                    sc.lookback, sc.max_tiles, err);
   return cudaGetLastError();
 }
 

@@ -52,6 +52,9 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
                               uint32_t* err, cudaStream_t stream);
 
+// Multiprocessors of the current device (cached per device).
+int sm_count();
+
 // Bytes of scratch needed for segments up to max_n keys (excluding nothing).
 size_t sort_scratch_bytes(uint32_t max_n);
 // Carves a SortScratch out of one device allocation of sort_scratch_bytes(max_n).
