@@ -129,6 +129,10 @@ typedef struct SkyStatus {
   uint64_t kernel_launches;   /* kernels launched by the context so far     */
   uint64_t graph_replays;     /* training steps run as a graph replay       */
   uint64_t graph_captures;    /* graph (re-)captures                        */
+  float scene_extent;         /* max bounding-box extent of the loaded points */
+  uint32_t scored_views;      /* views behind the current multi-view scores */
+  uint32_t densify_runs;      /* sky_densify calls that changed the scene   */
+  uint32_t prune_runs;        /* prunes that removed Gaussians              */
 } SkyStatus;
 
 /* Stages timed by sky_set_profiling / sky_get_stage_times, in order.  The
@@ -156,17 +160,67 @@ typedef struct SkyPruneParams {
   uint32_t reserved;
 } SkyPruneParams;
 
-/* Densify rule of performDensification (gaussian-renderer.ts:3248-3318). */
+/* Densify rule of performDensification (gaussian-renderer.ts:3248-3318):
+ * a Gaussian seen in >= min_visibility steps whose multi-view importance
+ * (error-pixel count / scored views) exceeds importance_threshold is cloned
+ * when max sigma <= size_threshold and its mean |dL/dmean2d| >=
+ * grad_threshold * pixel_width / 2, split when larger and its mean
+ * |dL/dconic| >= grad_abs_threshold * pixel_width / 2.  At most
+ * max(1, floor(max_new_ratio * N)) candidates, by descending normalised
+ * gradient, are applied.  sky_densify_default fills the reference values. */
 typedef struct SkyDensifyParams {
-  float grad_threshold;      /* 0.003 (scaled by width / 2)     */
-  float grad_abs_threshold;  /* 0.015 (scaled by width / 2)     */
-  float size_threshold;      /* dense_size_ratio * scene_extent */
-  float min_visibility;      /* 25                              */
-  float importance_threshold;/* candidates need importance > it */
-  float max_new_ratio;       /* 0.1                             */
-  float pixel_width;         /* training width for the scaling  */
+  float grad_threshold;      /* 0.003 (scaled by width / 2)           */
+  float grad_abs_threshold;  /* 0.015 (scaled by width / 2)           */
+  float size_threshold;      /* 0.001 * scene extent                  */
+  float min_visibility;      /* 25                                    */
+  float importance_threshold;/* 5 (MULTI_VIEW_IMPORTANCE_THRESHOLD)   */
+  float max_new_ratio;       /* 0.1                                   */
+  float pixel_width;         /* 0: width of camera 0                  */
   uint32_t reserved;
 } SkyDensifyParams;
+
+/* Multi-view weighted prune of applyMultiViewPrune (gaussian-renderer.ts:
+ * 2800-2915).  Prunable: sigmoid(logit) < min_opacity, max sigma >
+ * max_scale, or (use_screen_size) decayed max screen radius >
+ * max_screen_radius.  Each prunable Gaussian gets the weight
+ * 1 / (1e-6 + 1 - clamp(normalised pruning score + bonuses, 0, 0.999)) and
+ * min(prunable, max(1, floor(prune_ratio * prunable)),
+ *     max(1, floor(max_ratio * scored count))) of them are drawn without
+ * replacement with probability proportional to weight (seeded).          */
+typedef struct SkyScoredPruneParams {
+  float min_opacity;       /* 0.005                                     */
+  float max_scale;         /* 1.0 (maxScaleAbsolute)                    */
+  float max_screen_radius; /* 20 pixels                                 */
+  uint32_t use_screen_size;/* 1 after the first opacity reset           */
+  float prune_ratio;       /* 0.5  (MULTI_VIEW_PRUNE_RATIO)             */
+  float max_ratio;         /* 0.02 (MULTI_VIEW_PRUNE_MAX_RATIO)         */
+  float opacity_bonus;     /* 0.35                                      */
+  float scale_bonus;       /* 0.25                                      */
+  float screen_bonus;      /* 0.25                                      */
+  uint32_t use_last_scores;/* 1: use the last scores even if a densify
+                              has run since (runDensifyAndPruneCombined
+                              :3468-3490); 0: rescore if stale          */
+} SkyScoredPruneParams;
+
+/* Training schedule of TrainingController (src/utils/training-controller.ts:
+ * 23-160), run by sky_train after each step when enabled: densify (with
+ * the combined prune) every densify_interval steps in [densify_from,
+ * densify_until], otherwise prune every prune_interval steps in
+ * [prune_from, prune_until], and clamp opacities to opacity_reset_value
+ * every opacity_reset_interval steps inside the densify window.          */
+typedef struct SkySchedule {
+  uint32_t enabled;
+  uint32_t densify_from, densify_until, densify_interval;   /* 500, 15000, 100 */
+  uint32_t prune_from, prune_until, prune_interval;         /* 500, 25000, 100 */
+  uint32_t opacity_reset_interval;                          /* 3000            */
+  float opacity_reset_value;                                /* 0.01            */
+  float min_opacity;                                        /* 0.005           */
+  float max_screen_size;                                    /* 20              */
+  float max_scale_ratio;                                    /* 0               */
+  float max_scale_absolute;                                 /* 1.0             */
+  float scene_extent;                                       /* 0: from points  */
+  SkyDensifyParams densify;
+} SkySchedule;
 
 /* ---- buffers readable with sky_read_buffer (introspection) -------------- */
 #define SKY_BUF_RECORDS 1      /* per (view, Gaussian) raster record, 12 f32:
@@ -231,11 +285,33 @@ int sky_backward(void* ctx, float* grads, uint64_t plane_stride);
 int sky_step(void* ctx, const uint32_t* cameras, uint32_t n, SkyStepStats* stats);
 int sky_train(void* ctx, uint32_t iterations, uint32_t views_per_step, SkyStepStats* last);
 
-/* ---- prune / densify / opacity reset ------------------------------------ */
+/* ---- prune / densify / opacity reset ------------------------------------
+ * sky_prune: rule or mask prune without the random budget (prune-decide
+ * path), compaction as applyPruneMask (:2917-3000).
+ * sky_densify_stats: per Gaussian the densify accumulator (|dmean2d| sum, 0,
+ * |dconic| sum, count; densify-accum.wgsl) and the importance statistics
+ * (decayed tile count, visibility, max screen radius, 0;
+ * importance-accum.wgsl), 4 f32 each, gathered by every training step.
+ * sky_score_views: multi-view error scores (generateMultiViewScores
+ * :2758-2788) over the given cameras, or when cameras is NULL over
+ * min(10, cameras) drawn by the context's seeded generator; per Gaussian a
+ * u32 importance (error-pixel hits) and an f32 pruning score (hits x mean
+ * L1 of the view).  Scores are kept for sky_densify / sky_prune_scored in
+ * the same iteration (getMultiViewScores :2790-2798).
+ * sky_densify: clone/split on the device; new Gaussians are appended after
+ * the survivors with zero Adam moments; resets both statistics.
+ * sky_prune_scored: the weighted prune; resets both statistics.          */
 int sky_prune(void* ctx, const SkyPruneParams* p, const uint8_t* mask, uint32_t* removed);
-int sky_densify_stats(void* ctx, float* grad_accum, float* importance); /* 4 f32 each per G */
+int sky_densify_stats(void* ctx, float* grad_accum, float* importance);
+int sky_score_views(void* ctx, const uint32_t* cameras, uint32_t n, uint32_t* importance,
+                    float* pruning);
+void sky_densify_default(SkyDensifyParams* p);
 int sky_densify(void* ctx, const SkyDensifyParams* p, uint32_t* cloned, uint32_t* split);
+void sky_scored_prune_default(SkyScoredPruneParams* p);
+int sky_prune_scored(void* ctx, const SkyScoredPruneParams* p, uint32_t* removed);
 int sky_reset_opacity(void* ctx, float max_opacity);                   /* resetOpacity :3867 */
+void sky_schedule_default(SkySchedule* s);
+int sky_set_schedule(void* ctx, const SkySchedule* s);
 
 /* ---- readback ------------------------------------------------------------- */
 int sky_get_params(void* ctx, float* params, uint64_t plane_stride);

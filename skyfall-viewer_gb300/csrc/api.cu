@@ -17,6 +17,7 @@
 #include <string>
 #include <vector>
 
+#include "densify.cuh"
 #include "kernels.cuh"
 #include "skyfall.h"
 
@@ -124,6 +125,15 @@ struct Context {
   Buf keys, keys_sorted, vals_sorted, rec_of, flatten, partials, tile_grads, gsum54;
   Buf offsets, loss_partials, color, alpha, tfinal, last, residual, targets, sort_mem;
   Buf flags, flag_scan, d_sp, d_st;
+  // densification statistics (float4 per Gaussian) and multi-view scores
+  Buf imp_stats, dens_accum, score_imp, score_prune, score_counts, metric_l1, metric_part,
+      metric_stats;
+  bool scores_valid = false;  // scores belong to (scores_iter, current scene)
+  uint64_t scores_iter = 0;
+  uint32_t scores_n = 0, scores_views = 0;
+  float scene_extent = 1.0f;
+  SkySchedule sched{};
+  uint32_t densify_runs = 0, prune_runs = 0;
   SortScratch sort{};
   uint32_t icap = 0;
   std::vector<SkyCamera> cams;
@@ -189,6 +199,17 @@ void dev_free(Context* c, Buf& b) {
   b.bytes = 0;
 }
 
+// Zeroed densify accumulators and importance statistics for `stride`
+// Gaussians (resetAccumulators / resetStats after a load, densify or prune).
+int reset_stats(Context* c) {
+  const size_t bytes = (size_t)c->stride * 16;
+  TRY(dev_alloc(c, c->imp_stats, bytes));
+  TRY(dev_alloc(c, c->dens_accum, bytes));
+  CK(cudaMemsetAsync(c->imp_stats.p, 0, bytes, c->stream));
+  CK(cudaMemsetAsync(c->dens_accum.p, 0, bytes, c->stream));
+  return SKY_OK;
+}
+
 DevBuffers make_buffers(Context* c) {
   DevBuffers b{};
   b.params = (float*)c->params.p;
@@ -217,6 +238,8 @@ DevBuffers make_buffers(Context* c) {
   b.last = (uint32_t*)c->last.p;
   b.residual = (float4*)c->residual.p;
   b.targets = (const float4*)c->targets.p;
+  b.importance = (float*)c->imp_stats.p;
+  b.densify_accum = (float*)c->dens_accum.p;
   b.sp = (const StepParams*)c->d_sp.p;
   b.status = (DevStatus*)c->d_st.p;
   return b;
@@ -467,6 +490,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   sp.beta1 = cfg.beta1;
   sp.beta2 = cfg.beta2;
   sp.adam_eps = cfg.adam_eps;
+  sp.importance_decay = 0.98f;  // DEFAULT_IMPORTANCE_CONFIG.decay (importance.ts:9)
   {
     // run_adam_on_buffer (gaussian-renderer.ts:2420-2430): t = max(1, counter)
     const double t = (double)std::max<uint64_t>(1, c->adam_steps);
@@ -570,6 +594,366 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
 
 Context* as_ctx(void* p) { return (Context*)p; }
 
+// ---- densification, multi-view scores, scored prune ----------------------
+
+// Device buffer released when it goes out of scope.
+struct TempBuf {
+  Context* c;
+  Buf b;
+  explicit TempBuf(Context* ctx) : c(ctx) {}
+  ~TempBuf() {
+    if (b.p) dev_free(c, b);
+  }
+  template <class T>
+  T* as() const {
+    return (T*)b.p;
+  }
+};
+
+uint32_t stat_blocks(uint32_t n) {
+  return std::max<uint32_t>(1, std::min<uint32_t>((n + 255) / 256, (uint32_t)sm_count() * 4));
+}
+
+// sampleCameraIndices (gaussian-renderer.ts:2677-2688) over the cameras that
+// have a target: all of them in order when there are at most 10, else the
+// first 10 of a Fisher-Yates shuffle driven by the context's generator.
+std::vector<uint32_t> sample_cameras(Context* c) {
+  std::vector<uint32_t> idx;
+  for (uint32_t i = 0; i < (uint32_t)c->cams.size(); ++i)
+    if (c->tgt_set[i]) idx.push_back(i);
+  const size_t count = std::min<size_t>(10, idx.size());
+  if (count >= idx.size()) return idx;
+  for (size_t i = idx.size() - 1; i > 0; --i) {
+    const double u = (splitmix64(c->rng) >> 11) * (1.0 / 9007199254740992.0);
+    const size_t j = (size_t)(u * (double)(i + 1));
+    std::swap(idx[i], idx[j]);
+  }
+  idx.resize(count);
+  return idx;
+}
+
+// generateMultiViewScores (:2758-2788): render the views in batches, then
+// per view in order: L1 map, its statistics, error-pixel hits per Gaussian.
+int score_views(Context* c, const std::vector<uint32_t>& views) {
+  const uint32_t n = c->n;
+  for (uint32_t v : views) {
+    if (v >= c->cams.size()) return fail(SKY_ERR_ARG, "camera %u not set", v);
+    if (!c->tgt_set[v]) return fail(SKY_ERR_STATE, "camera %u has no target", v);
+  }
+  cudaStream_t s = c->stream;
+  TRY(dev_alloc(c, c->score_imp, (size_t)n * 4));
+  TRY(dev_alloc(c, c->score_prune, (size_t)n * 4));
+  TRY(dev_alloc(c, c->score_counts, (size_t)n * 4));
+  TRY(dev_alloc(c, c->metric_stats, (size_t)kMaxViews * sizeof(MetricStats)));
+  CK(cudaMemsetAsync(c->score_imp.p, 0, (size_t)n * 4, s));
+  CK(cudaMemsetAsync(c->score_prune.p, 0, (size_t)n * 4, s));
+  CK(cudaMemsetAsync(c->score_counts.p, 0, (size_t)n * 4, s));
+  MetricStats* st = (MetricStats*)c->metric_stats.p;
+  for (size_t first = 0; first < views.size(); first += kMaxViews) {
+    const uint32_t nb = (uint32_t)std::min<size_t>(kMaxViews, views.size() - first);
+    TRY(run_views(c, views.data() + first, nb, kRender, nullptr));
+    DevBuffers b = make_buffers(c);
+    for (uint32_t v = 0; v < nb; ++v) {
+      const ViewInfo& vi = c->h_sp->views[v];
+      const uint32_t npx = vi.width * vi.height;
+      const uint32_t blocks = stat_blocks(npx);
+      TRY(dev_alloc(c, c->metric_l1, (size_t)npx * 4));
+      // partials: blocks f32 minima, blocks f32 maxima, then (8-byte aligned)
+      // blocks f64 sums
+      TRY(dev_alloc(c, c->metric_part, (size_t)blocks * 16 + 8));
+      float* pmin = (float*)c->metric_part.p;
+      float* pmax = pmin + blocks;
+      double* psum = (double*)(pmax + blocks + (blocks & 1));
+      launch_metric_map(b.color, b.targets, vi.pixel_base, vi.target_base, npx,
+                        (float*)c->metric_l1.p, s);
+      launch_metric_stats((const float*)c->metric_l1.p, npx, pmin, pmax, psum, blocks, st + v, s);
+      launch_metric_accum(b, v, npx, (const float*)c->metric_l1.p, st + v, 0.1f,
+                          (uint32_t*)c->score_counts.p, s);
+      launch_metric_combine((uint32_t*)c->score_counts.p, n, st + v, (uint32_t*)c->score_imp.p,
+                            (float*)c->score_prune.p, s);
+      c->launches += 5;
+    }
+  }
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  c->scores_valid = true;
+  c->scores_iter = c->iteration;
+  c->scores_n = n;
+  c->scores_views = (uint32_t)views.size();
+  return SKY_OK;
+}
+
+// Scores of the current iteration and scene (getMultiViewScores cache),
+// computed from a seeded camera sample when missing.  *have = false when no
+// camera has a target (the reference skips densify and prune then).
+int current_scores(Context* c, bool* have) {
+  *have = true;
+  if (c->scores_valid && c->scores_iter == c->iteration && c->scores_n == c->n) return SKY_OK;
+  std::vector<uint32_t> views = sample_cameras(c);
+  if (views.empty()) {
+    *have = false;
+    return SKY_OK;
+  }
+  return score_views(c, views);
+}
+
+// Stable ascending order of n 64-bit keys given as (lo, hi) halves: two LSD
+// passes of 32-bit sorts.  order[k] = index of the k-th smallest key.
+int sort_keys64(Context* c, const uint32_t* lo, const uint32_t* hi, uint32_t n, uint32_t* order) {
+  cudaStream_t s = c->stream;
+  TempBuf mem(c), kout(c), ord1(c), hperm(c), err(c);
+  TRY(dev_alloc(c, mem.b, sort_scratch_bytes(n)));
+  TRY(dev_alloc(c, kout.b, (size_t)n * 4));
+  TRY(dev_alloc(c, ord1.b, (size_t)n * 4));
+  TRY(dev_alloc(c, hperm.b, (size_t)n * 4));
+  TRY(dev_alloc(c, err.b, 16));
+  CK(cudaMemsetAsync(err.b.p, 0, 16, s));
+  SortScratch sc = sort_scratch_carve(mem.b.p, n);
+  SortSegment seg{nullptr, n};
+  CK(sort_pairs_launch(lo, nullptr, kout.as<uint32_t>(), ord1.as<uint32_t>(), seg, n, 32, sc,
+                       err.as<uint32_t>(), s));
+  launch_gather_u32(hi, ord1.as<uint32_t>(), n, hperm.as<uint32_t>(), s);
+  CK(sort_pairs_launch(hperm.as<uint32_t>(), ord1.as<uint32_t>(), kout.as<uint32_t>(), order, seg, n,
+                       32, sc, err.as<uint32_t>(), s));
+  uint32_t e = 0;
+  CK(cudaMemcpyAsync(&e, err.b.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  c->launches += 11;
+  if (e & SKY_DEVERR_SORT_TIMEOUT) return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  return SKY_OK;
+}
+
+// Inclusive scan of n u32 flags into out (the hot path's scan kernels).
+int scan_flags(Context* c, const uint32_t* flags, uint32_t* out, uint32_t n) {
+  TempBuf bs(c);
+  TRY(dev_alloc(c, bs.b, ((size_t)scan_block_count(n) + 1) * 4));
+  DevBuffers sb{};
+  sb.counts = (uint32_t*)flags;
+  sb.cumsum = out;
+  sb.block_sums = bs.as<uint32_t>();
+  launch_scan(sb, n, c->stream);
+  c->launches += 3;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->stream));
+  return SKY_OK;
+}
+
+// After a change of the scene: statistics reset, cached scores stale.
+int scene_changed(Context* c, uint32_t n, uint32_t stride) {
+  if (c->grads.p) dev_free(c, c->grads);
+  c->n = n;
+  c->stride = stride;
+  c->fwd_ready = false;
+  c->scores_valid = false;
+  return reset_stats(c);
+}
+
+// Compacts params and moments to the survivors flagged 1 in keep
+// (applyPruneMask :2917-3000).
+int compact_survivors(Context* c, const uint32_t* keep, uint32_t keep_n) {
+  const uint32_t n = c->n;
+  cudaStream_t s = c->stream;
+  TempBuf scan(c);
+  TRY(dev_alloc(c, scan.b, (size_t)n * 4));
+  TRY(scan_flags(c, keep, scan.as<uint32_t>(), n));
+  const uint32_t new_stride = (keep_n + 255) & ~255u;
+  const size_t bytes = (size_t)kPlanes * new_stride * 4;
+  Buf* planes[3] = {&c->params, &c->m1, &c->m2};
+  for (Buf* pl : planes) {
+    Buf nb;
+    TRY(dev_alloc(c, nb, bytes));
+    launch_compact((const float*)pl->p, (float*)nb.p, c->stride, new_stride, kPlanes, n,
+                   scan.as<uint32_t>(), s);
+    ++c->launches;
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(s));
+    dev_free(c, *pl);
+    *pl = nb;
+  }
+  return scene_changed(c, keep_n, new_stride);
+}
+
+// performDensification (:3211-3433) on the device.
+int densify(Context* c, const SkyDensifyParams& prm, uint32_t* cloned, uint32_t* split) {
+  const uint32_t n = c->n;
+  if (n == 0) return SKY_OK;
+  if (n >= (1u << 30)) return fail(SKY_ERR_ARG, "densify supports fewer than 2^30 Gaussians");
+  cudaStream_t s = c->stream;
+  bool have = false;
+  TRY(current_scores(c, &have));
+  if (!have) {  // no multi-view scores: accumulators reset, nothing else
+    CK(cudaMemsetAsync(c->dens_accum.p, 0, (size_t)c->stride * 16, s));
+    CK(cudaStreamSynchronize(s));
+    return SKY_OK;
+  }
+  double width = prm.pixel_width;
+  if (!(width > 0.0)) {
+    const uint32_t cam = c->last_views.empty() ? 0u : c->last_views[0];
+    width = cam < c->cams.size() ? c->cams[cam].width : 1.0;
+  }
+  const double pixel_scale = std::max(width, 1.0) / 2.0;
+  DensifyRule rule{};
+  rule.grad_px = js_literal(prm.grad_threshold) * pixel_scale;
+  rule.grad_abs_px = js_literal(prm.grad_abs_threshold) * pixel_scale;
+  rule.size_threshold = prm.size_threshold > 0.0f ? (double)prm.size_threshold
+                                                  : (double)c->scene_extent * 0.001;
+  rule.min_visibility = std::max(1.0, (double)js_literal(prm.min_visibility));
+  rule.importance_threshold = js_literal(prm.importance_threshold);
+  rule.sample_count = (double)c->scores_views;
+  TempBuf action(c), klo(c), khi(c), order(c), keep(c), newc(c), kscan(c), nscan(c), cnt(c);
+  for (TempBuf* t : {&action, &klo, &khi, &order, &keep, &newc, &kscan, &nscan})
+    TRY(dev_alloc(c, t->b, (size_t)n * 4));
+  TRY(dev_alloc(c, cnt.b, 16));
+  CK(cudaMemsetAsync(cnt.b.p, 0, 16, s));
+  launch_densify_decide((const float*)c->params.p, c->stride, n, (const float4*)c->dens_accum.p,
+                        (const uint32_t*)c->score_imp.p, rule, action.as<uint32_t>(),
+                        klo.as<uint32_t>(), khi.as<uint32_t>(), cnt.as<uint32_t>(), s);
+  ++c->launches;
+  uint32_t ncand = 0;
+  CK(cudaMemcpyAsync(&ncand, cnt.b.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (ncand == 0) {
+    CK(cudaMemsetAsync(c->dens_accum.p, 0, (size_t)c->stride * 16, s));
+    CK(cudaStreamSynchronize(s));
+    return SKY_OK;
+  }
+  const uint64_t max_new = std::max<uint64_t>(1, (uint64_t)std::floor((double)n * js_literal(prm.max_new_ratio)));
+  const uint32_t allowed = (uint32_t)std::min<uint64_t>(max_new, ncand);
+  TRY(sort_keys64(c, klo.as<uint32_t>(), khi.as<uint32_t>(), n, order.as<uint32_t>()));
+  launch_densify_select(order.as<uint32_t>(), n, allowed, action.as<uint32_t>(), keep.as<uint32_t>(),
+                        newc.as<uint32_t>(), s);
+  ++c->launches;
+  TRY(scan_flags(c, keep.as<uint32_t>(), kscan.as<uint32_t>(), n));
+  TRY(scan_flags(c, newc.as<uint32_t>(), nscan.as<uint32_t>(), n));
+  uint32_t survivors = 0, added = 0;
+  CK(cudaMemcpyAsync(&survivors, kscan.as<uint32_t>() + (n - 1), 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(&added, nscan.as<uint32_t>() + (n - 1), 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const uint32_t splits = n - survivors, clones = added - 2 * splits;
+  const uint64_t new_n = (uint64_t)survivors + added;
+  if (new_n >= (1ull << 31)) return fail(SKY_ERR_CAPACITY, "densify would exceed 2^31 Gaussians");
+  const uint32_t new_stride = ((uint32_t)new_n + 255) & ~255u;
+  const size_t bytes = (size_t)kPlanes * new_stride * 4;
+  Buf np, nm1, nm2;
+  TRY(dev_alloc(c, np, bytes));
+  int rc = dev_alloc(c, nm1, bytes);
+  if (rc == SKY_OK) rc = dev_alloc(c, nm2, bytes);
+  if (rc != SKY_OK) {
+    dev_free(c, np);
+    dev_free(c, nm1);
+    return rc;
+  }
+  launch_densify_build((const float*)c->params.p, (const float*)c->m1.p, (const float*)c->m2.p,
+                       c->stride, n, kscan.as<uint32_t>(), nscan.as<uint32_t>(), survivors,
+                       (float*)np.p, (float*)nm1.p, (float*)nm2.p, new_stride, c->cfg.seed,
+                       c->iteration, s);
+  ++c->launches;
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(s));
+  dev_free(c, c->params);
+  dev_free(c, c->m1);
+  dev_free(c, c->m2);
+  c->params = np;
+  c->m1 = nm1;
+  c->m2 = nm2;
+  TRY(scene_changed(c, (uint32_t)new_n, new_stride));
+  c->densify_runs += 1;
+  if (cloned) *cloned = clones;
+  if (split) *split = splits;
+  return SKY_OK;
+}
+
+// applyMultiViewPrune (:2800-2915) on the device.
+int prune_scored(Context* c, const SkyScoredPruneParams& prm, uint32_t* removed) {
+  const uint32_t n = c->n;
+  if (n == 0) return SKY_OK;
+  if (n >= (1u << 30)) return fail(SKY_ERR_ARG, "prune supports fewer than 2^30 Gaussians");
+  cudaStream_t s = c->stream;
+  const bool last_ok = prm.use_last_scores && c->scores_n > 0 && c->score_prune.p;
+  if (!last_ok) {
+    bool have = false;
+    TRY(current_scores(c, &have));
+    if (!have) return SKY_OK;
+  }
+  if (c->scores_views == 0) return SKY_OK;
+  const uint32_t base = std::min(c->scores_n, n);
+  PruneRule rule{};
+  rule.min_opacity = js_literal(prm.min_opacity);
+  rule.max_scale = js_literal(prm.max_scale);
+  rule.max_screen_radius = js_literal(prm.max_screen_radius);
+  rule.opacity_bonus = js_literal(prm.opacity_bonus);
+  rule.scale_bonus = js_literal(prm.scale_bonus);
+  rule.screen_bonus = js_literal(prm.screen_bonus);
+  rule.use_screen = prm.use_screen_size && prm.max_screen_radius < 9999.0f ? 1u : 0u;
+  const uint32_t blocks = stat_blocks(base);
+  TempBuf norm(c), part(c), klo(c), khi(c), order(c), keep(c), cnt(c);
+  for (TempBuf* t : {&norm, &klo, &khi, &order, &keep}) TRY(dev_alloc(c, t->b, (size_t)n * 4));
+  TRY(dev_alloc(c, part.b, (size_t)blocks * 8));
+  TRY(dev_alloc(c, cnt.b, 16));
+  CK(cudaMemsetAsync(cnt.b.p, 0, 16, s));
+  launch_prune_normalise((const float*)c->score_prune.p, base, n, norm.as<float>(), part.as<float>(),
+                         part.as<float>() + blocks, blocks, s);
+  launch_prune_weights((const float*)c->params.p, c->stride, n, norm.as<float>(),
+                       (const float4*)c->imp_stats.p, rule, klo.as<uint32_t>(), khi.as<uint32_t>(),
+                       cnt.as<uint32_t>(), c->cfg.seed, c->iteration, s);
+  c->launches += 3;
+  uint32_t to_remove = 0;
+  CK(cudaMemcpyAsync(&to_remove, cnt.b.p, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (to_remove == 0) return SKY_OK;
+  const uint64_t max_removals =
+      std::max<uint64_t>(1, (uint64_t)std::floor((double)c->scores_n * js_literal(prm.max_ratio)));
+  const uint64_t desired =
+      std::max<uint64_t>(1, (uint64_t)std::floor((double)to_remove * js_literal(prm.prune_ratio)));
+  const uint32_t budget = (uint32_t)std::min<uint64_t>(to_remove, std::min(desired, max_removals));
+  if (budget >= n) return SKY_OK;  // applyPruneMask keeps at least one Gaussian
+  TRY(sort_keys64(c, klo.as<uint32_t>(), khi.as<uint32_t>(), n, order.as<uint32_t>()));
+  launch_prune_select(order.as<uint32_t>(), n, budget, keep.as<uint32_t>(), s);
+  ++c->launches;
+  TRY(compact_survivors(c, keep.as<uint32_t>(), n - budget));
+  c->prune_runs += 1;
+  if (removed) *removed = budget;
+  return SKY_OK;
+}
+
+// TrainingController.getIterationActions (training-controller.ts:85-160) and
+// the train loop's handling of it (gaussian-renderer.ts:3795-3829).
+int run_schedule(Context* c) {
+  const SkySchedule& sc = c->sched;
+  const uint64_t it = c->iteration;
+  const bool in_densify = it >= sc.densify_from && it <= sc.densify_until;
+  const double extent = sc.scene_extent > 0.0f ? (double)sc.scene_extent : (double)c->scene_extent;
+  SkyScoredPruneParams pp;
+  sky_scored_prune_default(&pp);
+  const bool screen = it > sc.opacity_reset_interval;
+  pp.min_opacity = sc.min_opacity;
+  pp.max_scale = sc.max_scale_absolute > 0.0f ? sc.max_scale_absolute
+                 : sc.max_scale_ratio > 0.0f  ? (float)(extent * js_literal(sc.max_scale_ratio))
+                                              : 1e6f;
+  pp.use_screen_size = screen ? 1u : 0u;
+  pp.max_screen_radius = screen ? sc.max_screen_size : 10000.0f;
+  bool prune_attempted = false;
+  if (in_densify && it % sc.densify_interval == 0) {
+    bool have = false;
+    TRY(current_scores(c, &have));
+    if (have) {
+      SkyDensifyParams dp = sc.densify;
+      if (!(dp.size_threshold > 0.0f)) dp.size_threshold = (float)(extent * 0.001);
+      TRY(densify(c, dp, nullptr, nullptr));
+      pp.use_last_scores = 1;
+      TRY(prune_scored(c, pp, nullptr));
+      prune_attempted = true;
+    }
+  }
+  if (!prune_attempted && it >= sc.prune_from && it <= sc.prune_until && it % sc.prune_interval == 0) {
+    pp.use_last_scores = 0;
+    TRY(prune_scored(c, pp, nullptr));
+  }
+  if (it != 0 && in_densify && it % sc.opacity_reset_interval == 0)
+    TRY(sky_reset_opacity(c, sc.opacity_reset_value));
+  return SKY_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -661,7 +1045,9 @@ int sky_destroy(void* p) {
                 &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->partials,
                 &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
-                &c->flag_scan, &c->d_sp, &c->d_st};
+                &c->flag_scan, &c->d_sp, &c->d_st, &c->imp_stats, &c->dens_accum,
+                &c->score_imp, &c->score_prune, &c->score_counts, &c->metric_l1,
+                &c->metric_part, &c->metric_stats};
   for (Buf* b : all) dev_free(c, *b);
   drop_graph(c);
   for (int k = 0; k <= SKY_NUM_STAGES; ++k)
@@ -721,6 +1107,9 @@ static int load_planes(Context* c, uint32_t n) {
   c->iteration = 0;
   c->adam_steps = 0;
   c->fwd_ready = false;
+  c->scores_valid = false;
+  c->scores_n = 0;
+  TRY(reset_stats(c));
   return SKY_OK;
 }
 
@@ -730,6 +1119,18 @@ int sky_load_points(void* p, const float* params, uint32_t n, uint64_t plane_str
   TRY(load_planes(c, n));
   CK(cudaMemcpy2DAsync(c->params.p, (size_t)c->stride * 4, params, (size_t)plane_stride * 4,
                        (size_t)n * 4, kPlanes, cudaMemcpyHostToDevice, c->stream));
+  // scene_extent = max bounding-box extent (pointcloud-loader.ts:103-106)
+  double ext = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    const float* v = params + (size_t)k * plane_stride;
+    float lo = v[0], hi = v[0];
+    for (uint32_t i = 1; i < n; ++i) {
+      lo = std::min(lo, v[i]);
+      hi = std::max(hi, v[i]);
+    }
+    ext = std::max(ext, (double)hi - (double)lo);
+  }
+  c->scene_extent = (float)ext;
   CK(cudaStreamSynchronize(c->stream));
   return SKY_OK;
 }
@@ -875,6 +1276,7 @@ int sky_train(void* p, uint32_t iterations, uint32_t views_per_step, SkyStepStat
     for (uint32_t k = 0; k < views_per_step; ++k)
       v[k] = (uint32_t)(((splitmix64(c->rng) >> 11) * (1.0 / 9007199254740992.0)) * c->cams.size());
     TRY(run_views(c, v.data(), views_per_step, kTrain, last));
+    if (c->sched.enabled) TRY(run_schedule(c));
   }
   return SKY_OK;
 }
@@ -925,6 +1327,10 @@ int sky_get_status(void* p, SkyStatus* st) {
   st->kernel_launches = c->launches;
   st->graph_replays = c->graph_replays;
   st->graph_captures = c->graph_captures;
+  st->scene_extent = c->scene_extent;
+  st->scored_views = c->scores_views;
+  st->densify_runs = c->densify_runs;
+  st->prune_runs = c->prune_runs;
   return SKY_OK;
 }
 
@@ -1068,16 +1474,111 @@ int sky_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* k
   return SKY_OK;
 }
 
-// Not yet implemented entry points report SKY_ERR_STATE.
-int sky_prune(void* p, const SkyPruneParams* prm, const uint8_t* mask, uint32_t* removed);
 int sky_densify_stats(void* p, float* grad_accum, float* importance) {
-  (void)p; (void)grad_accum; (void)importance;
-  return fail(SKY_ERR_STATE, "densify statistics are not implemented");
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (c->n == 0) return SKY_OK;
+  CK(cudaStreamSynchronize(c->stream));
+  if (grad_accum)
+    CK(cudaMemcpy(grad_accum, c->dens_accum.p, (size_t)c->n * 16, cudaMemcpyDeviceToHost));
+  if (importance)
+    CK(cudaMemcpy(importance, c->imp_stats.p, (size_t)c->n * 16, cudaMemcpyDeviceToHost));
+  return SKY_OK;
 }
+
+void sky_densify_default(SkyDensifyParams* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->grad_threshold = 0.003f;
+  p->grad_abs_threshold = 0.015f;
+  p->size_threshold = 0.0f;  // 0: 0.001 * scene extent
+  p->min_visibility = 25.0f;
+  p->importance_threshold = 5.0f;
+  p->max_new_ratio = 0.1f;
+  p->pixel_width = 0.0f;
+}
+
+void sky_scored_prune_default(SkyScoredPruneParams* p) {
+  if (!p) return;
+  memset(p, 0, sizeof(*p));
+  p->min_opacity = 0.005f;
+  p->max_scale = 1.0f;
+  p->max_screen_radius = 20.0f;
+  p->use_screen_size = 0;
+  p->prune_ratio = 0.5f;
+  p->max_ratio = 0.02f;
+  p->opacity_bonus = 0.35f;
+  p->scale_bonus = 0.25f;
+  p->screen_bonus = 0.25f;
+  p->use_last_scores = 0;
+}
+
+void sky_schedule_default(SkySchedule* s) {
+  if (!s) return;
+  memset(s, 0, sizeof(*s));
+  s->enabled = 1;
+  s->densify_from = 500;
+  s->densify_until = 15000;
+  s->densify_interval = 100;
+  s->prune_from = 500;
+  s->prune_until = 25000;
+  s->prune_interval = 100;
+  s->opacity_reset_interval = 3000;
+  s->opacity_reset_value = 0.01f;
+  s->min_opacity = 0.005f;
+  s->max_screen_size = 20.0f;
+  s->max_scale_ratio = 0.0f;
+  s->max_scale_absolute = 1.0f;
+  s->scene_extent = 0.0f;
+  sky_densify_default(&s->densify);
+}
+
+int sky_set_schedule(void* p, const SkySchedule* s) {
+  Context* c = as_ctx(p);
+  if (!c || !s) return fail(SKY_ERR_ARG, "bad schedule arguments");
+  if (s->enabled && (s->densify_interval == 0 || s->prune_interval == 0 || s->opacity_reset_interval == 0))
+    return fail(SKY_ERR_ARG, "schedule intervals must be positive");
+  c->sched = *s;
+  return SKY_OK;
+}
+
+int sky_score_views(void* p, const uint32_t* cams, uint32_t n, uint32_t* importance, float* pruning) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (c->n == 0) return fail(SKY_ERR_STATE, "no Gaussians loaded");
+  std::vector<uint32_t> list;
+  if (cams) {
+    if (n == 0) return fail(SKY_ERR_ARG, "no cameras to score");
+    list.assign(cams, cams + n);
+  } else {
+    list = sample_cameras(c);
+  }
+  if (list.empty()) return fail(SKY_ERR_STATE, "no cameras to score");
+  TRY(score_views(c, list));
+  if (importance)
+    CK(cudaMemcpy(importance, c->score_imp.p, (size_t)c->scores_n * 4, cudaMemcpyDeviceToHost));
+  if (pruning)
+    CK(cudaMemcpy(pruning, c->score_prune.p, (size_t)c->scores_n * 4, cudaMemcpyDeviceToHost));
+  return SKY_OK;
+}
+
 int sky_densify(void* p, const SkyDensifyParams* prm, uint32_t* cloned, uint32_t* split) {
-  (void)p; (void)prm; (void)cloned; (void)split;
-  return fail(SKY_ERR_STATE, "densify is not implemented");
+  Context* c = as_ctx(p);
+  if (cloned) *cloned = 0;
+  if (split) *split = 0;
+  if (!c || !prm) return fail(SKY_ERR_ARG, "bad densify arguments");
+  if (!(prm->max_new_ratio >= 0.0f) || !(prm->min_visibility >= 0.0f))
+    return fail(SKY_ERR_ARG, "negative densify ratio or visibility");
+  return densify(c, *prm, cloned, split);
 }
+
+int sky_prune_scored(void* p, const SkyScoredPruneParams* prm, uint32_t* removed) {
+  Context* c = as_ctx(p);
+  if (removed) *removed = 0;
+  if (!c || !prm) return fail(SKY_ERR_ARG, "bad prune arguments");
+  return prune_scored(c, *prm, removed);
+}
+
 int sky_reset_opacity(void* p, float max_opacity);
 
 }  // extern "C"
@@ -1097,8 +1598,6 @@ extern "C" int sky_prune(void* p, const SkyPruneParams* prm, const uint8_t* mask
     CK(cudaMemcpyAsync(dmask.p, mask, n, cudaMemcpyHostToDevice, s));
   }
   TRY(dev_alloc(c, c->flags, (size_t)n * 4));
-  TRY(dev_alloc(c, c->flag_scan, (size_t)n * 4));
-  TRY(dev_alloc(c, c->block_sums, (scan_block_count(n) + 1) * 4));
   const float min_op = prm ? prm->min_opacity : 0.0f;
   const float max_scale = prm ? prm->max_scale : INFINITY;
   launch_prune_flags((const float*)c->params.p, c->stride, n, min_op, max_scale,
@@ -1123,29 +1622,8 @@ extern "C" int sky_prune(void* p, const SkyPruneParams* prm, const uint8_t* mask
   // applyPruneMask (gaussian-renderer.ts:2917-2925): nothing to do when no
   // Gaussian or every Gaussian would be removed.
   if (remove == 0 || remove >= n) return SKY_OK;
-  DevBuffers sb{};
-  sb.counts = (uint32_t*)c->flags.p;
-  sb.cumsum = (uint32_t*)c->flag_scan.p;
-  sb.block_sums = (uint32_t*)c->block_sums.p;
-  launch_scan(sb, n, s);
-  const uint32_t keep_n = (uint32_t)(n - remove);
-  uint32_t new_stride = (keep_n + 255) & ~255u;
-  const size_t bytes = (size_t)kPlanes * new_stride * 4;
-  Buf* planes[3] = {&c->params, &c->m1, &c->m2};
-  for (Buf* pl : planes) {
-    Buf nb;
-    TRY(dev_alloc(c, nb, bytes));
-    launch_compact((const float*)pl->p, (float*)nb.p, c->stride, new_stride, kPlanes, n,
-                   (const uint32_t*)c->flag_scan.p, s);
-    CK(cudaGetLastError());
-    CK(cudaStreamSynchronize(s));
-    dev_free(c, *pl);
-    *pl = nb;
-  }
-  if (c->grads.p) dev_free(c, c->grads);
-  c->n = keep_n;
-  c->stride = new_stride;
-  c->fwd_ready = false;
+  TRY(compact_survivors(c, (const uint32_t*)c->flags.p, (uint32_t)(n - remove)));
+  c->prune_runs += 1;
   if (removed) *removed = (uint32_t)remove;
   return SKY_OK;
 }

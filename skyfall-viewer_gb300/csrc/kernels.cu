@@ -1075,9 +1075,28 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   for (int k = 0; k < 4; ++k) gr.q[k] = 0.f;
   gr.logit = 0.f;
   auto get = [&](int plane) { return plane < 11 ? prm[plane] : s_sh[plane - 11][t]; };
+  // Densification statistics of training steps, per view in view order:
+  // importance-accum.wgsl:19-40 (decayed tile count, visibility, screen
+  // radius) and densify-accum.wgsl:19-46 (|dL/dmean2d|, |dL/dconic|, count).
+  const bool stats = sp.apply_adam != 0 && b.importance != nullptr;
+  float4 imp = make_float4(0.f, 0.f, 0.f, 0.f), acc = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (stats) {
+    imp = reinterpret_cast<const float4*>(b.importance)[g];
+    acc = reinterpret_cast<const float4*>(b.densify_accum)[g];
+  }
   for (uint32_t v = 0; v < sp.num_views; ++v) {
     const size_t item = (size_t)v * sp.n + g;
     const uint32_t cnt = b.counts[item];
+    if (stats) {
+      imp.x = imp.x * sp.importance_decay;
+      imp.y = imp.y * sp.importance_decay;
+      imp.z = imp.z * sp.importance_decay;
+      if (cnt > 0u) {
+        imp.x = imp.x + (float)cnt;
+        imp.y = imp.y + 1.0f;
+        imp.z = fmax_(imp.z, b.aux[item].y);
+      }
+    }
     if (cnt == 0) continue;
     float in9[9];
 #pragma unroll
@@ -1123,6 +1142,17 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
         if (need_sh_grads) s_gsh[k][t] += (float)q * sc;
       }
     }
+    if (stats) {
+      const float n2d = sqrtf(in9[7] * in9[7] + in9[8] * in9[8]);
+      float nc = in9[4] * in9[4] + in9[5] * in9[5];
+      nc = sqrtf(nc + in9[6] * in9[6]);
+      if (n2d > 1e-10f || nc > 1e-10f) {
+        acc.x = acc.x + n2d;
+        acc.y = 0.0f;
+        acc.z = acc.z + nc;
+        acc.w = acc.w + 1.0f;
+      }
+    }
     if (!any) continue;
     const ViewInfo& vi = sp.views[v];
     ProjOut o;
@@ -1139,6 +1169,10 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
           if (k < ncoef) s_gsh[3 * k + c][t] += Y[k] * dr;
       }
     }
+  }
+  if (stats) {
+    reinterpret_cast<float4*>(b.importance)[g] = imp;
+    reinterpret_cast<float4*>(b.densify_accum)[g] = acc;
   }
   float g11[11] = {gr.pos[0], gr.pos[1], gr.pos[2], gr.ls[0], gr.ls[1], gr.ls[2],
                    gr.q[0],   gr.q[1],   gr.q[2],   gr.q[3],  gr.logit};

@@ -50,7 +50,7 @@ struct StepParams {
   float w_l2, w_l1, w_ssim, pad1;
   float lr_pos, lr_scale, lr_rot, lr_opacity;
   float lr_sh, beta1, beta2, adam_eps;
-  float bc1_rcp, bc2_sqrt_rcp, pad2, pad3;
+  float bc1_rcp, bc2_sqrt_rcp, importance_decay, pad3;
   GroupInfo groups[kMaxGroups];
   ViewInfo views[kMaxViews];
 };

@@ -87,7 +87,9 @@ class SkyStatus(C.Structure):
                 ("last_intersections", C.c_uint64), ("device_bytes", C.c_uint64),
                 ("num_gaussians", C.c_uint32), ("capacity", C.c_uint32), ("num_cameras", C.c_uint32),
                 ("error_flags", C.c_uint32), ("kernel_launches", C.c_uint64),
-                ("graph_replays", C.c_uint64), ("graph_captures", C.c_uint64)]
+                ("graph_replays", C.c_uint64), ("graph_captures", C.c_uint64),
+                ("scene_extent", C.c_float), ("scored_views", C.c_uint32),
+                ("densify_runs", C.c_uint32), ("prune_runs", C.c_uint32)]
 
 
 STAGES = ["preprocess", "scan", "emit", "sort", "ranges", "forward", "backward", "geom_adam"]
@@ -103,6 +105,25 @@ class SkyDensifyParams(C.Structure):
                 ("size_threshold", C.c_float), ("min_visibility", C.c_float),
                 ("importance_threshold", C.c_float), ("max_new_ratio", C.c_float),
                 ("pixel_width", C.c_float), ("reserved", C.c_uint32)]
+
+
+class SkyScoredPruneParams(C.Structure):
+    _fields_ = [("min_opacity", C.c_float), ("max_scale", C.c_float),
+                ("max_screen_radius", C.c_float), ("use_screen_size", C.c_uint32),
+                ("prune_ratio", C.c_float), ("max_ratio", C.c_float),
+                ("opacity_bonus", C.c_float), ("scale_bonus", C.c_float),
+                ("screen_bonus", C.c_float), ("use_last_scores", C.c_uint32)]
+
+
+class SkySchedule(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("densify_from", C.c_uint32),
+                ("densify_until", C.c_uint32), ("densify_interval", C.c_uint32),
+                ("prune_from", C.c_uint32), ("prune_until", C.c_uint32),
+                ("prune_interval", C.c_uint32), ("opacity_reset_interval", C.c_uint32),
+                ("opacity_reset_value", C.c_float), ("min_opacity", C.c_float),
+                ("max_screen_size", C.c_float), ("max_scale_ratio", C.c_float),
+                ("max_scale_absolute", C.c_float), ("scene_extent", C.c_float),
+                ("densify", SkyDensifyParams)]
 
 
 P = C.c_void_p
@@ -132,6 +153,12 @@ PROTOTYPES = {
     "sky_prune": (I32, [P, C.POINTER(SkyPruneParams), P, C.POINTER(U32)]),
     "sky_densify_stats": (I32, [P, P, P]),
     "sky_densify": (I32, [P, C.POINTER(SkyDensifyParams), C.POINTER(U32), C.POINTER(U32)]),
+    "sky_densify_default": (None, [C.POINTER(SkyDensifyParams)]),
+    "sky_score_views": (I32, [P, P, U32, P, P]),
+    "sky_scored_prune_default": (None, [C.POINTER(SkyScoredPruneParams)]),
+    "sky_prune_scored": (I32, [P, C.POINTER(SkyScoredPruneParams), C.POINTER(U32)]),
+    "sky_schedule_default": (None, [C.POINTER(SkySchedule)]),
+    "sky_set_schedule": (I32, [P, C.POINTER(SkySchedule)]),
     "sky_reset_opacity": (I32, [P, C.c_float]),
     "sky_get_params": (I32, [P, P, U64]),
     "sky_get_moments": (I32, [P, P, P, U64]),

@@ -194,6 +194,74 @@ class GaussianRenderer:
     def resetOpacity(self, maxOpacity: float = 0.1) -> None:
         L.check(self._L.sky_reset_opacity(self._h, maxOpacity))
 
+    def densifyStats(self) -> tuple[np.ndarray, np.ndarray]:
+        """(grad_accum, importance_stats), each (N, 4) f32: the densify
+        accumulator and the importance statistics the training steps gather."""
+        n = self.getGaussianCount()
+        g = np.zeros((n, 4), np.float32)
+        i = np.zeros((n, 4), np.float32)
+        L.check(self._L.sky_densify_stats(self._h, L.ptr(g), L.ptr(i)))
+        return g, i
+
+    def scoreViews(self, cameras=None) -> tuple[np.ndarray, np.ndarray]:
+        """Multi-view scores (generateMultiViewScores): per Gaussian the u32
+        error-pixel hits and the f32 pruning score; cameras=None samples
+        min(10, cameras) with the context's seeded generator."""
+        n = self.getGaussianCount()
+        imp = np.zeros(n, np.uint32)
+        pr = np.zeros(n, np.float32)
+        if cameras is None:
+            L.check(self._L.sky_score_views(self._h, None, 0, L.ptr(imp), L.ptr(pr)))
+        else:
+            cams = np.ascontiguousarray(np.atleast_1d(cameras), dtype=np.uint32)
+            L.check(self._L.sky_score_views(self._h, L.ptr(cams), len(cams), L.ptr(imp), L.ptr(pr)))
+        return imp, pr
+
+    @staticmethod
+    def densifyParams(**overrides) -> L.SkyDensifyParams:
+        p = L.SkyDensifyParams()
+        L.lib().sky_densify_default(C.byref(p))
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        return p
+
+    def densify(self, params: L.SkyDensifyParams | None = None, **overrides) -> tuple[int, int]:
+        """performDensification: returns (cloned, split)."""
+        p = params if params is not None else self.densifyParams(**overrides)
+        cl, sp = C.c_uint32(), C.c_uint32()
+        L.check(self._L.sky_densify(self._h, C.byref(p), C.byref(cl), C.byref(sp)))
+        return cl.value, sp.value
+
+    @staticmethod
+    def scoredPruneParams(**overrides) -> L.SkyScoredPruneParams:
+        p = L.SkyScoredPruneParams()
+        L.lib().sky_scored_prune_default(C.byref(p))
+        for k, v in overrides.items():
+            setattr(p, k, v)
+        return p
+
+    def pruneScored(self, params: L.SkyScoredPruneParams | None = None, **overrides) -> int:
+        """applyMultiViewPrune: returns the number of Gaussians removed."""
+        p = params if params is not None else self.scoredPruneParams(**overrides)
+        removed = C.c_uint32()
+        L.check(self._L.sky_prune_scored(self._h, C.byref(p), C.byref(removed)))
+        return removed.value
+
+    def setSchedule(self, enabled: bool = True, **overrides) -> L.SkySchedule:
+        """TrainingController schedule run by train(): densify/prune/opacity
+        reset windows and thresholds (defaults of DEFAULT_TRAINING_SCHEDULE)."""
+        s = L.SkySchedule()
+        L.lib().sky_schedule_default(C.byref(s))
+        s.enabled = 1 if enabled else 0
+        for k, v in overrides.items():
+            if k == "densify":
+                for dk, dv in v.items():
+                    setattr(s.densify, dk, dv)
+            else:
+                setattr(s, k, v)
+        L.check(self._L.sky_set_schedule(self._h, C.byref(s)))
+        return s
+
     # -- parameters and status ---------------------------------------------
     def getTrainingParams(self) -> TrainingParams:
         c = self.config
