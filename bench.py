@@ -142,6 +142,23 @@ def measured_peak():
     return 6800.0, "fallback"
 
 
+def max_over_ranks(value: float, world: int, device: str = "cuda") -> float:
+    """The largest `value` over the replicas (the slowest rank's time).  The
+    replicas train independent copies: nothing else crosses ranks."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_throughput(views_per_rank: int, world: int, ms_max: float) -> float:
+    """Whole-job views/s: every rank's views over the slowest rank's time."""
+    return views_per_rank * world / (ms_max / 1000.0)
+
+
 def time_steps(r, torch, view_sets, warmup):
     """Device time (CUDA events on the library stream) of len(view_sets)
     sky_step calls after `warmup` untimed ones; also wall clock."""
@@ -260,16 +277,11 @@ def main():
     with Clocks(local) as clk:
         res = time_steps(r, torch, batched_sets, 0)
     barrier()
-    ms = res["ms"]
-    if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    views_done = args.steps * B * world
-    value = views_done / (ms / 1000.0)
+    ms = max_over_ranks(res["ms"], world)
+    value = replica_throughput(args.steps * B, world, ms)
     px_per_view = args.width * args.height
     mpix = value * px_per_view / 1e6
-    e2e_value = args.steps * B / res["wall"] * world
+    e2e_value = replica_throughput(args.steps * B, world, max_over_ranks(res["wall"] * 1000.0, world))
 
     plain = None
     plain_stage_ms = None
