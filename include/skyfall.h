@@ -313,6 +313,27 @@ int sky_reset_opacity(void* ctx, float max_opacity);                   /* resetO
 void sky_schedule_default(SkySchedule* s);
 int sky_set_schedule(void* ctx, const SkySchedule* s);
 
+/* ---- headless viewer frame --------------------------------------------------
+ * The viewer path of frame(encoder, view) (gaussian-renderer.ts:4111-4123):
+ * preprocess.wgsl:116-204 per Gaussian, a global back-to-front depth sort,
+ * and one quad of half-width ceil(3 sqrt(lambda_max)) per splat blended
+ * "over" (src-alpha, one-minus-src-alpha; gaussian.wgsl:15-67) into a target
+ * cleared to transparent black.  The swapchain texture becomes an f32 RGBA
+ * buffer (W x H x 4, row-major, y down); rgba8, if given, receives it
+ * converted as round(clamp(v, 0, 1) * 255).  Either pointer may be NULL (the
+ * image stays readable as SKY_BUF_VIEW_RGBA).  Camera: view, proj, focal and
+ * the viewport size (width, height) as in SkyCamera.                       */
+typedef struct SkyViewSettings {
+  float gaussian_scaling;     /* RenderSettings.gaussian_scaling, 1.0      */
+  uint32_t sh_degree;         /* RenderSettings.sh_deg, 0..3               */
+  uint32_t round_params_f16;  /* 1: parameters read through f16 storage   */
+  uint32_t reserved;
+} SkyViewSettings;
+#define SKY_BUF_VIEW_RGBA 19  /* last viewer frame, 4 f32 per pixel */
+void sky_view_settings_default(SkyViewSettings* s);
+int sky_view_render(void* ctx, const SkyCamera* camera, const SkyViewSettings* s, float* rgba,
+                    uint8_t* rgba8);
+
 /* ---- readback ------------------------------------------------------------- */
 int sky_get_params(void* ctx, float* params, uint64_t plane_stride);
 int sky_get_moments(void* ctx, float* m1, float* m2, uint64_t plane_stride);

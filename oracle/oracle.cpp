@@ -1180,4 +1180,159 @@ double orc_loss_f64(const double* params, uint64_t stride, uint32_t n, const Orc
   return loss;
 }
 
+// ---------------------------------------------------------------------------
+// Viewer frame (gaussian-renderer.ts:4111-4123): preprocess.wgsl:116-204 per
+// Gaussian, a stable ascending sort of float_to_ordered_uint(-z_camera)
+// (:94-98; the reference's atomic compaction order is replaced by index
+// order), then one quad per splat drawn in that order (gaussian.wgsl:15-67)
+// and blended with src-alpha / one-minus-src-alpha for colour and one /
+// one-minus-src-alpha for alpha (gaussian-renderer.ts:863-868) into an f32
+// target cleared to zero.  A pixel is covered when its centre lies in
+// [cx - r, cx + r) x [cy - r, cy + r) (top-left rule).
+// splats12: per Gaussian {cx, cy, a, b, c, opacity, r, g, b, radius, 0, 0};
+// keys: sort key per Gaussian (0xFFFFFFFF when culled).
+// ---------------------------------------------------------------------------
+int orc_view_render(const float* params, uint64_t stride, uint32_t n, const OrcCam* cam_in,
+                    float scaling, uint32_t sh_deg, uint32_t round16, float* rgba,
+                    float* splats12, uint32_t* keys_out) {
+  Cam cam = to_cam(cam_in);
+  const int deg = (int)std::min(sh_deg, 3u);
+  std::vector<float> sp((size_t)n * 12, 0.0f);
+  std::vector<uint32_t> key(n, 0xFFFFFFFFu);
+  for (uint32_t g = 0; g < n; ++g) {
+    auto get = [&](int plane) { return load_param<float>(params, stride, plane, g, round16 != 0); };
+    float p[3] = {get(0), get(1), get(2)};
+    float pc[4], clip[4];
+    cam_space<float>(cam, p, pc);
+    mat4_vec<float>(cam.proj, pc, clip);
+    const float w = clip[3];
+    const float ndc_x = clip[0] / w, ndc_y = clip[1] / w;
+    if (std::fabs(ndc_x) > 1.2f || std::fabs(ndc_y) > 1.2f || pc[2] < 0.0f) continue;  // :143
+    const float opacity = 1.0f / (1.0f + sky_expf(-get(10)));                          // :146
+    float sig[3];
+    for (int k = 0; k < 3; ++k)                                                       // :149-156
+      sig[k] = scaling * sky_expf(std::min(std::max(get(3 + k), -10.0f), 10.0f));
+    float q[4] = {get(6), get(7), get(8), get(9)};                                    // :159
+    float qq = q[0] * q[0] + q[1] * q[1];
+    qq = qq + q[2] * q[2];
+    qq = qq + q[3] * q[3];
+    const float ql = std::sqrt(qq);
+    const float rx = q[0] / ql, ry = q[1] / ql, rz = q[2] / ql, rw = q[3] / ql;
+    float R[3][3];  // quat_to_mat3 (:100-107), R[col][row]
+    R[0][0] = 1.0f - 2.0f * (ry * ry + rz * rz);
+    R[0][1] = 2.0f * (rx * ry - rw * rz);
+    R[0][2] = 2.0f * (rx * rz + rw * ry);
+    R[1][0] = 2.0f * (rx * ry + rw * rz);
+    R[1][1] = 1.0f - 2.0f * (rx * rx + rz * rz);
+    R[1][2] = 2.0f * (ry * rz - rw * rx);
+    R[2][0] = 2.0f * (rx * rz - rw * ry);
+    R[2][1] = 2.0f * (ry * rz + rw * rx);
+    R[2][2] = 1.0f - 2.0f * (rx * rx + ry * ry);
+    float A[3][3], C3[3][3];  // C3D = transpose(S R) S R (:163)
+    for (int j = 0; j < 3; ++j)
+      for (int r = 0; r < 3; ++r) A[j][r] = (sig[j] * R[r][j]) * sig[j];
+    for (int j = 0; j < 3; ++j)
+      for (int r = 0; r < 3; ++r) {
+        float acc = A[0][r] * R[j][0];
+        acc = acc + A[1][r] * R[j][1];
+        acc = acc + A[2][r] * R[j][2];
+        C3[j][r] = acc;
+      }
+    const float tx = pc[0], ty = pc[1], tz = pc[2];                                   // :165-176
+    const float fx = cam.focal[0], fy = cam.focal[1];
+    const float tz2 = tz * tz;
+    const float J00 = fx / tz, J11 = fy / tz;
+    const float J02 = -(fx * tx) / tz2, J12 = -(fy * ty) / tz2;
+    float T[3][3];
+    for (int j = 0; j < 3; ++j) {
+      const float v0 = cam.view[j * 4 + 0], v1 = cam.view[j * 4 + 1];
+      T[j][0] = J00 * v0;
+      T[j][1] = J11 * v1;
+      T[j][2] = J02 * v0 + J12 * v1;
+    }
+    float B0[3], B1[3];
+    for (int j = 0; j < 3; ++j) {
+      float a0 = T[0][0] * C3[j][0];
+      a0 = a0 + T[1][0] * C3[j][1];
+      a0 = a0 + T[2][0] * C3[j][2];
+      B0[j] = a0;
+      float a1 = T[0][1] * C3[j][0];
+      a1 = a1 + T[1][1] * C3[j][1];
+      a1 = a1 + T[2][1] * C3[j][2];
+      B1[j] = a1;
+    }
+    float c00 = B0[0] * T[0][0];
+    c00 = c00 + B0[1] * T[1][0];
+    c00 = c00 + B0[2] * T[2][0];
+    float c11 = B1[0] * T[0][1];
+    c11 = c11 + B1[1] * T[1][1];
+    c11 = c11 + B1[2] * T[2][1];
+    float c01 = B1[0] * T[0][0];
+    c01 = c01 + B1[1] * T[1][0];
+    c01 = c01 + B1[2] * T[2][0];
+    c00 = c00 + 0.3f;                                                                  // :179-180
+    c11 = c11 + 0.3f;
+    const float det = c00 * c11 - c01 * c01;
+    if (det <= 0.0f) continue;
+    const float det_inv = 1.0f / det;                                                  // :185-188
+    const float ca = c11 * det_inv, cb = (-c01) * det_inv, cc = c00 * det_inv;
+    float v[3] = {-pc[0], -pc[1], -pc[2]};                                             // :190
+    float vv = v[0] * v[0] + v[1] * v[1];
+    vv = vv + v[2] * v[2];
+    const float vl = std::sqrt(vv);
+    float sh[48], raw[3];
+    for (int k = 0; k < 48; ++k) sh[k] = get(11 + k);
+    sh_color<float>(sh, v[0] / vl, v[1] / vl, v[2] / vl, deg, raw);
+    const float mid = 0.5f * (c00 + c11);                                              // :194-198
+    const float disc = std::sqrt(std::max(mid * mid - det, 0.0f));
+    const float l1 = mid + disc, l2 = mid - disc;
+    const float radius = std::ceil(3.0f * std::sqrt(std::max(l1, l2)));
+    // gaussian.wgsl:27: center_px = (ndc * (0.5, -0.5) + 0.5) * viewport
+    const float cx = (ndc_x * 0.5f + 0.5f) * (float)cam.width;
+    const float cy = (ndc_y * -0.5f + 0.5f) * (float)cam.height;
+    float* o = &sp[(size_t)g * 12];
+    o[0] = cx; o[1] = cy; o[2] = ca; o[3] = cb; o[4] = cc; o[5] = opacity;
+    for (int c = 0; c < 3; ++c) o[6 + c] = std::max(0.0f, raw[c]);
+    o[9] = radius;
+    const uint32_t bits = f2u(-pc[2]);
+    key[g] = bits ^ ((bits & 0x80000000u) ? 0xFFFFFFFFu : 0x80000000u);
+  }
+  std::vector<uint32_t> order;
+  for (uint32_t g = 0; g < n; ++g)
+    if (key[g] != 0xFFFFFFFFu) order.push_back(g);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](uint32_t a, uint32_t b) { return key[a] < key[b]; });
+  const uint32_t W = cam.width, H = cam.height;
+  std::fill(rgba, rgba + (size_t)W * H * 4, 0.0f);
+  for (uint32_t g : order) {
+    const float* s = &sp[(size_t)g * 12];
+    const float cx = s[0], cy = s[1], r = s[9];
+    const float X0 = cx - r, X1 = cx + r, Y0 = cy - r, Y1 = cy + r;
+    if (!(X1 > 0.0f) || !(Y1 > 0.0f) || !(X0 < (float)W) || !(Y0 < (float)H)) continue;
+    const int xlo = (int)std::max(std::floor(X0 - 0.5f) - 1.0f, 0.0f);
+    const int ylo = (int)std::max(std::floor(Y0 - 0.5f) - 1.0f, 0.0f);
+    const int xhi = (int)std::min(std::ceil(X1 - 0.5f) + 1.0f, (float)W - 1.0f);
+    const int yhi = (int)std::min(std::ceil(Y1 - 0.5f) + 1.0f, (float)H - 1.0f);
+    for (int y = ylo; y <= yhi; ++y)
+      for (int x = xlo; x <= xhi; ++x) {
+        const float px = (float)x + 0.5f, py = (float)y + 0.5f;
+        if (!(px >= cx - r && px < cx + r && py >= cy - r && py < cy + r)) continue;
+        const float dx = px - cx, dy = py - cy;                                       // fs_main
+        float so2 = 0.5f * ((s[2] * dx) * dx + (s[4] * dy) * dy);
+        so2 = so2 + (s[3] * dx) * dy;
+        if (so2 < 0.0f) continue;
+        const float a = std::min(std::max(s[5] * sky_expf(-so2), 0.0f), 1.0f);
+        const float om = 1.0f - a;
+        float* d = &rgba[((size_t)y * W + x) * 4];
+        d[0] = s[6] * a + d[0] * om;
+        d[1] = s[7] * a + d[1] * om;
+        d[2] = s[8] * a + d[2] * om;
+        d[3] = a + d[3] * om;
+      }
+  }
+  if (splats12) std::memcpy(splats12, sp.data(), sp.size() * sizeof(float));
+  if (keys_out) std::memcpy(keys_out, key.data(), key.size() * sizeof(uint32_t));
+  return 0;
+}
+
 }  // extern "C"

@@ -62,6 +62,8 @@ def lib():
         L.orc_loss_f64.restype = C.c_double
         L.orc_expf.argtypes = [P, P, C.c_uint64]
         L.orc_round_f16.argtypes = [P, P, C.c_uint64]
+        L.orc_view_render.argtypes = [P, C.c_uint64, C.c_uint32, P, C.c_float, C.c_uint32,
+                                      C.c_uint32, P, P, P]
         _lib = L
     return _lib
 
@@ -221,6 +223,20 @@ def loss_f64(params64: np.ndarray, cam: dict, s: OrcSettings, sh_deg: int, targe
     c = cam_struct(cam)
     v = lib().orc_loss_f64(ptr(p), n, n, C.byref(c), C.byref(s), sh_deg, ptr(t), C.byref(sig))
     return v, sig.value
+
+
+def view_render(params: np.ndarray, cam: dict, scaling: float = 1.0, sh_deg: int = 3,
+                round16: int = 1) -> dict:
+    """Viewer frame: rgba (H*W, 4) f32, per-Gaussian splat records and keys."""
+    params = np.ascontiguousarray(params, np.float32)
+    n = params.shape[1]
+    P = cam["width"] * cam["height"]
+    out = dict(rgba=np.empty((P, 4), np.float32), splats=np.empty((n, 12), np.float32),
+               keys=np.empty(n, np.uint32))
+    c = cam_struct(cam)
+    lib().orc_view_render(ptr(params), C.c_uint64(n), n, C.byref(c), C.c_float(scaling), sh_deg,
+                          round16, ptr(out["rgba"]), ptr(out["splats"]), ptr(out["keys"]))
+    return out
 
 
 def view_pipeline(params, cam, target, s: OrcSettings, sh_deg: int, mode: int = 0) -> dict:

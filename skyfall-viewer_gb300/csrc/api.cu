@@ -20,6 +20,7 @@
 #include "densify.cuh"
 #include "kernels.cuh"
 #include "skyfall.h"
+#include "viewer.cuh"
 
 using namespace sky;
 
@@ -134,6 +135,10 @@ struct Context {
   float scene_extent = 1.0f;
   SkySchedule sched{};
   uint32_t densify_runs = 0, prune_runs = 0;
+  // headless viewer frame
+  Buf v_splats, v_keys, v_counts, v_rects, v_order, v_ksorted, v_cum, v_csorted, v_bsums, v_misc,
+      v_tkeys, v_gidx, v_tkeys_s, v_gidx_s, v_offsets, v_rgba, v_sort;
+  uint32_t view_w = 0, view_h = 0;
   SortScratch sort{};
   uint32_t icap = 0;
   std::vector<SkyCamera> cams;
@@ -1047,7 +1052,10 @@ int sky_destroy(void* p) {
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
                 &c->flag_scan, &c->d_sp, &c->d_st, &c->imp_stats, &c->dens_accum,
                 &c->score_imp, &c->score_prune, &c->score_counts, &c->metric_l1,
-                &c->metric_part, &c->metric_stats};
+                &c->metric_part, &c->metric_stats, &c->v_splats, &c->v_keys, &c->v_counts,
+                &c->v_rects, &c->v_order, &c->v_ksorted, &c->v_cum, &c->v_csorted, &c->v_bsums,
+                &c->v_misc, &c->v_tkeys, &c->v_gidx, &c->v_tkeys_s, &c->v_gidx_s, &c->v_offsets,
+                &c->v_rgba, &c->v_sort};
   for (Buf* b : all) dev_free(c, *b);
   drop_graph(c);
   for (int k = 0; k <= SKY_NUM_STAGES; ++k)
@@ -1357,6 +1365,7 @@ int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* siz
     case SKY_BUF_RESIDUAL: src = c->residual.p; sz = P * 16; break;
     case SKY_BUF_PARTIALS: src = c->partials.p; sz = I * kPartialF4 * 16; break;
     case SKY_BUF_TILE_GRADS: src = c->tile_grads.p; sz = c->tile_grads.p ? I * 54 * 4 : 0; break;
+    case SKY_BUF_VIEW_RGBA: src = c->v_rgba.p; sz = (uint64_t)c->view_w * c->view_h * 16; break;
     case SKY_BUF_GRADS:
       src = c->grads.p;
       sz = c->grads.p ? (uint64_t)kPlanes * c->n * 4 : 0;
@@ -1580,6 +1589,123 @@ int sky_prune_scored(void* p, const SkyScoredPruneParams* prm, uint32_t* removed
 }
 
 int sky_reset_opacity(void* p, float max_opacity);
+
+void sky_view_settings_default(SkyViewSettings* s) {
+  if (!s) return;
+  memset(s, 0, sizeof(*s));
+  s->gaussian_scaling = 1.0f;
+  s->sh_degree = 3;
+  s->round_params_f16 = 1;
+}
+
+int sky_view_render(void* p, const SkyCamera* cam, const SkyViewSettings* vs, float* rgba,
+                    uint8_t* rgba8) {
+  Context* c = as_ctx(p);
+  if (!c || !cam || !vs) return fail(SKY_ERR_ARG, "bad view arguments");
+  if (cam->width == 0 || cam->height == 0 || cam->width > 65535u * kViewTile ||
+      cam->height > 65535u * kViewTile)
+    return fail(SKY_ERR_ARG, "viewport %ux%u out of range", cam->width, cam->height);
+  if (c->n == 0) return fail(SKY_ERR_STATE, "no Gaussians loaded");
+  const uint32_t n = c->n;
+  cudaStream_t s = c->stream;
+  ViewerParams vp{};
+  memcpy(vp.view, cam->view, sizeof(vp.view));
+  memcpy(vp.proj, cam->proj, sizeof(vp.proj));
+  vp.focal[0] = cam->focal[0];
+  vp.focal[1] = cam->focal[1];
+  vp.viewport[0] = (float)cam->width;
+  vp.viewport[1] = (float)cam->height;
+  vp.gaussian_scaling = vs->gaussian_scaling;
+  vp.sh_deg = vs->sh_degree;
+  vp.round_f16 = vs->round_params_f16;
+  vp.n = n;
+  vp.plane_stride = c->stride;
+  vp.width = cam->width;
+  vp.height = cam->height;
+  vp.tiles_x = (cam->width + kViewTile - 1) / kViewTile;
+  vp.tiles_y = (cam->height + kViewTile - 1) / kViewTile;
+  const uint32_t tiles = vp.tiles_x * vp.tiles_y;
+  const uint64_t px = (uint64_t)cam->width * cam->height;
+  // per Gaussian: project, sort by depth key, counts in depth order, scan
+  TRY(dev_alloc(c, c->v_splats, (size_t)n * 48));
+  TRY(dev_alloc(c, c->v_keys, (size_t)n * 4));
+  TRY(dev_alloc(c, c->v_counts, (size_t)n * 4));
+  TRY(dev_alloc(c, c->v_rects, (size_t)n * 8));
+  TRY(dev_alloc(c, c->v_order, (size_t)n * 4));
+  TRY(dev_alloc(c, c->v_ksorted, (size_t)n * 4));
+  TRY(dev_alloc(c, c->v_cum, (size_t)n * 4));
+  TRY(dev_alloc(c, c->v_csorted, (size_t)n * 4));
+  TRY(dev_alloc(c, c->v_bsums, ((size_t)scan_block_count(n) + 1) * 4));
+  TRY(dev_alloc(c, c->v_misc, 64));
+  TRY(dev_alloc(c, c->v_offsets, ((size_t)tiles + 1) * 4));
+  TRY(dev_alloc(c, c->v_rgba, px * 16));
+  unsigned long long* d_total = (unsigned long long*)c->v_misc.p;
+  uint32_t* d_err = (uint32_t*)((char*)c->v_misc.p + 8);
+  CK(cudaMemsetAsync(c->v_misc.p, 0, 64, s));
+  launch_viewer_project(vp, (const float*)c->params.p, (float4*)c->v_splats.p, (uint32_t*)c->v_keys.p,
+                        (uint32_t*)c->v_counts.p, (uint2*)c->v_rects.p, d_total, s);
+  unsigned long long total = 0;
+  CK(cudaMemcpyAsync(&total, d_total, 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (total >= (1ull << 30)) return fail(SKY_ERR_CAPACITY, "%llu quad-tile pairs exceed 2^30", total);
+  const uint32_t I = (uint32_t)total;
+  TRY(dev_alloc(c, c->v_sort, sort_scratch_bytes(std::max(n, std::max(I, 1u)))));
+  SortScratch sc = sort_scratch_carve(c->v_sort.p, std::max(n, std::max(I, 1u)));
+  SortSegment seg_n{nullptr, n};
+  CK(sort_pairs_launch((const uint32_t*)c->v_keys.p, nullptr, (uint32_t*)c->v_ksorted.p,
+                       (uint32_t*)c->v_order.p, seg_n, n, 32, sc, d_err, s));
+  launch_viewer_gather_counts((const uint32_t*)c->v_order.p, (const uint32_t*)c->v_counts.p, n,
+                              (uint32_t*)c->v_csorted.p, s);
+  DevBuffers sb{};
+  sb.counts = (uint32_t*)c->v_csorted.p;
+  sb.cumsum = (uint32_t*)c->v_cum.p;
+  sb.block_sums = (uint32_t*)c->v_bsums.p;
+  launch_scan(sb, n, s);
+  c->launches += 8;
+  // per quad-tile pair: emit in depth order, stable sort by tile, ranges
+  if (I > 0) {
+    TRY(dev_alloc(c, c->v_tkeys, (size_t)I * 4));
+    TRY(dev_alloc(c, c->v_gidx, (size_t)I * 4));
+    TRY(dev_alloc(c, c->v_tkeys_s, (size_t)I * 4));
+    TRY(dev_alloc(c, c->v_gidx_s, (size_t)I * 4));
+    launch_viewer_emit(vp, (const uint32_t*)c->v_order.p, (const uint32_t*)c->v_cum.p,
+                       (const uint32_t*)c->v_csorted.p, (const uint2*)c->v_rects.p, n,
+                       (uint32_t*)c->v_tkeys.p, (uint32_t*)c->v_gidx.p, s);
+    SortSegment seg_i{nullptr, I};
+    const uint32_t bits = std::max<uint32_t>(1, ceil_log2(tiles));
+    CK(sort_pairs_launch((const uint32_t*)c->v_tkeys.p, (const uint32_t*)c->v_gidx.p,
+                         (uint32_t*)c->v_tkeys_s.p, (uint32_t*)c->v_gidx_s.p, seg_i, I, bits, sc,
+                         d_err, s));
+    c->launches += 6;
+  }
+  launch_viewer_ranges(I ? (const uint32_t*)c->v_tkeys_s.p : nullptr, I, tiles,
+                       (uint32_t*)c->v_offsets.p, s);
+  launch_viewer_raster(vp, (const float4*)c->v_splats.p, (const uint32_t*)c->v_offsets.p,
+                       I ? (const uint32_t*)c->v_gidx_s.p : nullptr, (float4*)c->v_rgba.p, s);
+  c->launches += 2;
+  CK(cudaGetLastError());
+  uint32_t err = 0;
+  CK(cudaMemcpyAsync(&err, d_err, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (err & SKY_DEVERR_SORT_TIMEOUT) return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  c->view_w = cam->width;
+  c->view_h = cam->height;
+  if (rgba || rgba8) {
+    std::vector<float> tmp;
+    float* dst = rgba;
+    if (!dst) {
+      tmp.resize(px * 4);
+      dst = tmp.data();
+    }
+    CK(cudaMemcpy(dst, c->v_rgba.p, px * 16, cudaMemcpyDeviceToHost));
+    if (rgba8)
+      for (uint64_t i = 0; i < px * 4; ++i) {
+        const float v = std::min(std::max(dst[i], 0.0f), 1.0f);
+        rgba8[i] = (uint8_t)std::lround(v * 255.0f);
+      }
+  }
+  return SKY_OK;
+}
 
 }  // extern "C"
 

@@ -194,6 +194,25 @@ class GaussianRenderer:
     def resetOpacity(self, maxOpacity: float = 0.1) -> None:
         L.check(self._L.sky_reset_opacity(self._h, maxOpacity))
 
+    def frame(self, camera, gaussian_scaling: float = 1.0, sh_degree: int | None = None,
+              round_params_f16: bool = True, as_u8: bool = False) -> np.ndarray:
+        """frame(encoder, view) of the viewer, headless: the (H, W, 4) RGBA
+        image (f32, or u8 with as_u8) of the quad-splat render from `camera`."""
+        cam = to_sky_camera(camera)
+        vs = L.SkyViewSettings()
+        L.lib().sky_view_settings_default(C.byref(vs))
+        vs.gaussian_scaling = gaussian_scaling
+        vs.sh_degree = self.config.sh_degree if sh_degree is None else sh_degree
+        vs.round_params_f16 = 1 if round_params_f16 else 0
+        h, w = int(cam.height), int(cam.width)
+        if as_u8:
+            out = np.empty((h, w, 4), np.uint8)
+            L.check(self._L.sky_view_render(self._h, C.byref(cam), C.byref(vs), None, L.ptr(out)))
+        else:
+            out = np.empty((h, w, 4), np.float32)
+            L.check(self._L.sky_view_render(self._h, C.byref(cam), C.byref(vs), L.ptr(out), None))
+        return out
+
     def densifyStats(self) -> tuple[np.ndarray, np.ndarray]:
         """(grad_accum, importance_stats), each (N, 4) f32: the densify
         accumulator and the importance statistics the training steps gather."""
