@@ -266,6 +266,30 @@ int sky_camera_pinhole(const float view[16], double fx, double fy, double cx,
  * words, SH = 24 u32 words, common.wgsl:39-43).                              */
 int sky_load_points(void* ctx, const float* params, uint32_t n, uint64_t plane_stride);
 int sky_load_packed(void* ctx, const uint32_t* gaussians, const uint32_t* sh, uint32_t n);
+/* sky_load_ply replaces loadPlyFile / load() (src/utils/dataset-loader.ts:19,
+ * src/utils/load.ts:14-172, src/utils/plyreader.ts): binary little-endian
+ * PLY, 3DGS layout (f_dc_*, f_rest_*, opacity, scale_*, rot_0 = w) or xyz
+ * (+ rgb) point clouds with the reference's defaults; values are stored
+ * through f16 as the reference's packed buffers hold them.  n_out and
+ * sh_degree_out (may be NULL) receive the count and the file's SH degree;
+ * the scene extent becomes the max bounding-box extent of the positions.
+ * sky_save_ply writes the 3DGS layout (f32; rot_0 = w) for coefficients up
+ * to sh_degree -- it has no counterpart in the reference.
+ * sky_save_checkpoint / sky_load_checkpoint store and restore the whole
+ * training state (parameters, Adam moments, densification statistics,
+ * iteration and Adam counters, the camera-choice generator): training
+ * resumed from a checkpoint continues bit for bit as if uninterrupted.
+ * They have no counterpart in the reference.                               */
+int sky_load_ply(void* ctx, const char* path, uint32_t* n_out, uint32_t* sh_degree_out);
+/* The same import into host memory, without a context or a GPU: call with
+ * planes == NULL for the count, then with room for 59 * n floats (plane p of
+ * Gaussian i at planes[p * n + i]).  extent_out (may be NULL) receives the
+ * scene extent.                                                             */
+int sky_ply_read_host(const char* path, uint32_t* n_out, uint32_t* sh_degree_out, float* planes,
+                      uint64_t capacity_floats, double* extent_out);
+int sky_save_ply(void* ctx, const char* path, uint32_t sh_degree);
+int sky_save_checkpoint(void* ctx, const char* path);
+int sky_load_checkpoint(void* ctx, const char* path);
 int sky_set_cameras(void* ctx, const SkyCamera* cams, uint32_t n);  /* setTrainingCameras :4084 */
 int sky_set_target(void* ctx, uint32_t camera, const float* rgb, uint32_t width,
                    uint32_t height);                                /* setTrainingImages :4098 */

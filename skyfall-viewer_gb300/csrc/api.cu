@@ -19,6 +19,7 @@
 
 #include "densify.cuh"
 #include "kernels.cuh"
+#include "plyio.cuh"
 #include "skyfall.h"
 #include "viewer.cuh"
 
@@ -1188,6 +1189,127 @@ int sky_load_packed(void* p, const uint32_t* gaussians, const uint32_t* sh, uint
     }
   }
   return sky_load_points(p, planes.data(), n, n);
+}
+
+int sky_load_ply(void* p, const char* path, uint32_t* n_out, uint32_t* deg_out) {
+  Context* c = as_ctx(p);
+  if (!c || !path) return fail(SKY_ERR_ARG, "bad PLY arguments");
+  PlyScene sc;
+  std::string err;
+  if (ply_read(path, sc, err) != 0) return fail(SKY_ERR_ARG, "%s", err.c_str());
+  TRY(sky_load_points(p, sc.planes.data(), sc.n, sc.n));
+  c->scene_extent = (float)sc.extent;
+  if (n_out) *n_out = sc.n;
+  if (deg_out) *deg_out = sc.sh_deg;
+  return SKY_OK;
+}
+
+int sky_ply_read_host(const char* path, uint32_t* n_out, uint32_t* deg_out, float* planes,
+                      uint64_t capacity, double* extent_out) {
+  if (!path) return fail(SKY_ERR_ARG, "null path");
+  PlyScene sc;
+  std::string err;
+  if (ply_read(path, sc, err) != 0) return fail(SKY_ERR_ARG, "%s", err.c_str());
+  if (n_out) *n_out = sc.n;
+  if (deg_out) *deg_out = sc.sh_deg;
+  if (extent_out) *extent_out = sc.extent;
+  if (planes) {
+    if (capacity < sc.planes.size())
+      return fail(SKY_ERR_ARG, "planes hold %llu floats, need %zu", (unsigned long long)capacity,
+                  sc.planes.size());
+    memcpy(planes, sc.planes.data(), sc.planes.size() * sizeof(float));
+  }
+  return SKY_OK;
+}
+
+int sky_save_ply(void* p, const char* path, uint32_t sh_degree) {
+  Context* c = as_ctx(p);
+  if (!c || !path) return fail(SKY_ERR_ARG, "bad PLY arguments");
+  if (c->n == 0) return fail(SKY_ERR_STATE, "no Gaussians loaded");
+  std::vector<float> planes((size_t)kPlanes * c->n);
+  TRY(sky_get_params(p, planes.data(), c->n));
+  std::string err;
+  if (ply_write(path, planes.data(), c->n, c->n, sh_degree, err) != 0)
+    return fail(SKY_ERR_ARG, "%s", err.c_str());
+  return SKY_OK;
+}
+
+namespace {
+struct CkptHeader {
+  char magic[8];  // "SKYCKPT1"
+  uint32_t version, n, planes, reserved0;
+  uint64_t iteration, adam_steps, rng;
+  float scene_extent;
+  uint32_t densify_runs, prune_runs, reserved1;
+};
+}  // namespace
+
+int sky_save_checkpoint(void* p, const char* path) {
+  Context* c = as_ctx(p);
+  if (!c || !path) return fail(SKY_ERR_ARG, "bad checkpoint arguments");
+  if (c->n == 0) return fail(SKY_ERR_STATE, "no Gaussians loaded");
+  const uint32_t n = c->n;
+  CkptHeader h{};
+  memcpy(h.magic, "SKYCKPT1", 8);
+  h.version = 1;
+  h.n = n;
+  h.planes = kPlanes;
+  h.iteration = c->iteration;
+  h.adam_steps = c->adam_steps;
+  h.rng = c->rng;
+  h.scene_extent = c->scene_extent;
+  h.densify_runs = c->densify_runs;
+  h.prune_runs = c->prune_runs;
+  std::vector<float> P((size_t)kPlanes * n), M1(P.size()), M2(P.size()), I4((size_t)n * 4), G4(I4.size());
+  TRY(sky_get_params(p, P.data(), n));
+  TRY(sky_get_moments(p, M1.data(), M2.data(), n));
+  TRY(sky_densify_stats(p, G4.data(), I4.data()));
+  FILE* f = fopen(path, "wb");
+  if (!f) return fail(SKY_ERR_ARG, "cannot create %s", path);
+  bool ok = fwrite(&h, sizeof(h), 1, f) == 1;
+  for (const std::vector<float>* v : {&P, &M1, &M2, &I4, &G4})
+    ok = ok && fwrite(v->data(), 4, v->size(), f) == v->size();
+  if (fclose(f) != 0) ok = false;
+  if (!ok) return fail(SKY_ERR_ARG, "write failed: %s", path);
+  return SKY_OK;
+}
+
+int sky_load_checkpoint(void* p, const char* path) {
+  Context* c = as_ctx(p);
+  if (!c || !path) return fail(SKY_ERR_ARG, "bad checkpoint arguments");
+  FILE* f = fopen(path, "rb");
+  if (!f) return fail(SKY_ERR_ARG, "cannot open %s", path);
+  CkptHeader h{};
+  bool ok = fread(&h, sizeof(h), 1, f) == 1;
+  if (!ok || memcmp(h.magic, "SKYCKPT1", 8) != 0 || h.version != 1 || h.planes != (uint32_t)kPlanes ||
+      h.n == 0 || h.n >= (1u << 31)) {
+    fclose(f);
+    return fail(SKY_ERR_ARG, "%s is not a version-1 skyfall checkpoint", path);
+  }
+  const uint32_t n = h.n;
+  std::vector<float> P((size_t)kPlanes * n), M1(P.size()), M2(P.size()), I4((size_t)n * 4), G4(I4.size());
+  for (std::vector<float>* v : {&P, &M1, &M2, &I4, &G4}) ok = ok && fread(v->data(), 4, v->size(), f) == v->size();
+  fclose(f);
+  if (!ok) return fail(SKY_ERR_ARG, "%s is truncated", path);
+  TRY(load_planes(c, n));
+  cudaStream_t s = c->stream;
+  const size_t pitch = (size_t)c->stride * 4;
+  CK(cudaMemcpy2DAsync(c->params.p, pitch, P.data(), (size_t)n * 4, (size_t)n * 4, kPlanes,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpy2DAsync(c->m1.p, pitch, M1.data(), (size_t)n * 4, (size_t)n * 4, kPlanes,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpy2DAsync(c->m2.p, pitch, M2.data(), (size_t)n * 4, (size_t)n * 4, kPlanes,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->imp_stats.p, I4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->dens_accum.p, G4.data(), (size_t)n * 16, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
+  c->iteration = h.iteration;
+  c->adam_steps = h.adam_steps;
+  c->rng = h.rng;
+  c->scene_extent = h.scene_extent;
+  c->densify_runs = h.densify_runs;
+  c->prune_runs = h.prune_runs;
+  return SKY_OK;
 }
 
 int sky_set_cameras(void* p, const SkyCamera* cams, uint32_t n) {

@@ -148,6 +148,12 @@ PROTOTYPES = {
                                  C.POINTER(SkyCamera)]),
     "sky_load_points": (I32, [P, P, U32, U64]),
     "sky_load_packed": (I32, [P, P, P, U32]),
+    "sky_load_ply": (I32, [P, C.c_char_p, C.POINTER(U32), C.POINTER(U32)]),
+    "sky_save_ply": (I32, [P, C.c_char_p, U32]),
+    "sky_ply_read_host": (I32, [C.c_char_p, C.POINTER(U32), C.POINTER(U32), P, U64,
+                                C.POINTER(C.c_double)]),
+    "sky_save_checkpoint": (I32, [P, C.c_char_p]),
+    "sky_load_checkpoint": (I32, [P, C.c_char_p]),
     "sky_set_cameras": (I32, [P, C.POINTER(SkyCamera), U32]),
     "sky_set_target": (I32, [P, U32, P, U32, U32]),
     "sky_render": (I32, [P, P, U32, P, P]),
@@ -207,6 +213,17 @@ def check(rc: int) -> None:
 
 def ptr(a: np.ndarray | None):
     return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def read_ply(path) -> tuple[np.ndarray, int, float]:
+    """The PLY import into host memory (no GPU needed): ((59, N) f32 planes,
+    SH degree of the file, scene extent)."""
+    n, d, ext = C.c_uint32(), C.c_uint32(), C.c_double()
+    b = str(path).encode()
+    check(lib().sky_ply_read_host(b, C.byref(n), C.byref(d), None, 0, C.byref(ext)))
+    planes = np.empty((SKY_NUM_PLANES, n.value), np.float32)
+    check(lib().sky_ply_read_host(b, C.byref(n), C.byref(d), ptr(planes), planes.size, C.byref(ext)))
+    return planes, d.value, ext.value
 
 
 def default_config(**overrides) -> SkyConfig:

@@ -106,6 +106,21 @@ class GaussianRenderer:
         s = None if sh is None else np.ascontiguousarray(sh, dtype=np.uint32)
         L.check(self._L.sky_load_packed(self._h, L.ptr(g), L.ptr(s), g.shape[0]))
 
+    def loadPly(self, path) -> tuple[int, int]:
+        """loadPlyFile + reloadPointCloud: returns (N, SH degree of the file)."""
+        n, d = C.c_uint32(), C.c_uint32()
+        L.check(self._L.sky_load_ply(self._h, str(path).encode(), C.byref(n), C.byref(d)))
+        return n.value, d.value
+
+    def savePly(self, path, sh_degree: int = 3) -> None:
+        L.check(self._L.sky_save_ply(self._h, str(path).encode(), sh_degree))
+
+    def saveCheckpoint(self, path) -> None:
+        L.check(self._L.sky_save_checkpoint(self._h, str(path).encode()))
+
+    def loadCheckpoint(self, path) -> None:
+        L.check(self._L.sky_load_checkpoint(self._h, str(path).encode()))
+
     def setTrainingCameras(self, cameras) -> None:
         self._cams = [to_sky_camera(c) for c in cameras]
         arr = (L.SkyCamera * len(self._cams))(*self._cams)
