@@ -290,6 +290,15 @@ int sky_ply_read_host(const char* path, uint32_t* n_out, uint32_t* sh_degree_out
 int sky_save_ply(void* ctx, const char* path, uint32_t sh_degree);
 int sky_save_checkpoint(void* ctx, const char* path);
 int sky_load_checkpoint(void* ctx, const char* path);
+/* sky_knn_init replaces initializeKnnAndSync (gaussian-renderer.ts:2131-2171,
+ * knn-init.wgsl:40-90): per Gaussian the mean distance to its three nearest
+ * other Gaussians (positions through f16), sigma = min(clamp(max(mean / 3,
+ * 0.0015 E), 0.0007 E, 0.007 E), 0.1) with E = scene_extent (0: the
+ * context's), and every parameter re-read through f16 with log sigma in
+ * the three scale planes.  density_out (n floats, may be NULL) receives the
+ * mean distances.  Exact nearest neighbours from a uniform grid instead of
+ * the reference's all-pairs scan; results are identical.                  */
+int sky_knn_init(void* ctx, float scene_extent, float* density_out);
 int sky_set_cameras(void* ctx, const SkyCamera* cams, uint32_t n);  /* setTrainingCameras :4084 */
 int sky_set_target(void* ctx, uint32_t camera, const float* rgb, uint32_t width,
                    uint32_t height);                                /* setTrainingImages :4098 */

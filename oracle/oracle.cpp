@@ -68,6 +68,38 @@ float sky_expf(float x) {
   return u2f(f2u(p) + (kbits << 23));
 }
 
+// log(x): x = m 2^e, m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s) with
+// s = (m - 1) / (m + 1), odd series to s^11 by Horner in s^2 with fused
+// multiply-adds; log x = e ln2 (split hi/lo) + log m.  Within 2 ulp.
+float sky_logf(float x) {
+  if (x != x || x < 0.0f) return NAN;
+  if (x == 0.0f) return -INFINITY;
+  if (x == INFINITY) return x;
+  uint32_t b = f2u(x);
+  int e = 0;
+  if (b < 0x00800000u) {
+    x = x * 8388608.0f;
+    b = f2u(x);
+    e = -23;
+  }
+  e += (int)(b >> 23) - 127;
+  float m = u2f((b & 0x007FFFFFu) | 0x3F800000u);
+  if (m > 1.41421354f) {
+    m = m * 0.5f;
+    e += 1;
+  }
+  const float s = (m - 1.0f) / (m + 1.0f);
+  const float z = s * s;
+  float p = 0.181818187f;
+  p = std::fmaf(p, z, 0.222222224f);
+  p = std::fmaf(p, z, 0.285714298f);
+  p = std::fmaf(p, z, 0.400000006f);
+  p = std::fmaf(p, z, 0.666666687f);
+  const float lm = std::fmaf(s * z, p, 2.0f * s);
+  const float fe = (float)e;
+  return std::fmaf(fe, 0.693147182f, std::fmaf(fe, -1.90465421e-09f, lm));
+}
+
 // f32 -> f16 -> f32 with round-to-nearest-even (pack2x16float/unpack2x16float).
 float round_f16(float f) {
   uint32_t x = f2u(f);
@@ -492,6 +524,51 @@ void orc_expf(const float* x, float* y, uint64_t n) {
 }
 void orc_round_f16(const float* x, float* y, uint64_t n) {
   for (uint64_t i = 0; i < n; ++i) y[i] = round_f16(x[i]);
+}
+void orc_logf(const float* x, float* y, uint64_t n) {
+  for (uint64_t i = 0; i < n; ++i) y[i] = sky_logf(x[i]);
+}
+
+// knn_init (knn-init.wgsl:40-90) by brute force, as the reference runs it:
+// positions read through f16, the three smallest distances to the other
+// points (insert_sorted, strict <, starting at 1e10), their mean, sigma =
+// min(clamp(max(mean / 3, bias), lo, hi), 0.1) with lo / hi / bias =
+// extent x (0.0007, 0.007, 0.0015) in f32, log sigma stored through f16.
+// Outputs per point: density (mean distance) and the f16 log sigma.
+void orc_knn_init(const float* params, uint64_t stride, uint32_t n, float extent, float* density,
+                  float* log_sigma, uint32_t nthreads) {
+  std::vector<float> pos((size_t)n * 3);
+  for (uint32_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) pos[(size_t)i * 3 + k] = round_f16(params[(uint64_t)k * stride + i]);
+  const float lo_s = extent * 0.0007f, hi_s = extent * 0.007f, bias = extent * 0.0015f;
+  parallel_for(n, nthreads, [&](uint32_t i) {
+    float d[3] = {1e10f, 1e10f, 1e10f};
+    const float* p = &pos[(size_t)i * 3];
+    for (uint32_t j = 0; j < n; ++j) {
+      if (j == i) continue;
+      const float* q = &pos[(size_t)j * 3];
+      const float dx = p[0] - q[0], dy = p[1] - q[1], dz = p[2] - q[2];
+      float s = dx * dx + dy * dy;
+      s = s + dz * dz;
+      const float dist = std::sqrt(s);
+      if (dist < d[0]) {
+        d[2] = d[1];
+        d[1] = d[0];
+        d[0] = dist;
+      } else if (dist < d[1]) {
+        d[2] = d[1];
+        d[1] = dist;
+      } else if (dist < d[2]) {
+        d[2] = dist;
+      }
+    }
+    const float mean = ((d[0] + d[1]) + d[2]) / 3.0f;
+    float sig = std::max(mean / 3.0f, bias);
+    sig = std::min(std::max(sig, lo_s), hi_s);
+    sig = std::min(sig, 0.1f);
+    if (density) density[i] = mean;
+    log_sigma[i] = round_f16(sky_logf(std::max(sig, 1e-6f)));
+  });
 }
 
 // Projection of n Gaussians for one camera.  rec12: 12 f32 per Gaussian

@@ -64,6 +64,8 @@ def lib():
         L.orc_round_f16.argtypes = [P, P, C.c_uint64]
         L.orc_view_render.argtypes = [P, C.c_uint64, C.c_uint32, P, C.c_float, C.c_uint32,
                                       C.c_uint32, P, P, P]
+        L.orc_logf.argtypes = [P, P, C.c_uint64]
+        L.orc_knn_init.argtypes = [P, C.c_uint64, C.c_uint32, C.c_float, P, P, C.c_uint32]
         _lib = L
     return _lib
 
@@ -223,6 +225,24 @@ def loss_f64(params64: np.ndarray, cam: dict, s: OrcSettings, sh_deg: int, targe
     c = cam_struct(cam)
     v = lib().orc_loss_f64(ptr(p), n, n, C.byref(c), C.byref(s), sh_deg, ptr(t), C.byref(sig))
     return v, sig.value
+
+
+def logf(x: np.ndarray) -> np.ndarray:
+    x = np.ascontiguousarray(x, np.float32)
+    y = np.empty_like(x)
+    lib().orc_logf(ptr(x), ptr(y), x.size)
+    return y
+
+
+def knn_init(params: np.ndarray, extent: float, nthreads: int | None = None):
+    """All-pairs k-NN init: (density, f16 log sigma) per Gaussian."""
+    params = np.ascontiguousarray(params, np.float32)
+    n = params.shape[1]
+    dens = np.empty(n, np.float32)
+    ls = np.empty(n, np.float32)
+    lib().orc_knn_init(ptr(params), C.c_uint64(n), n, C.c_float(extent), ptr(dens), ptr(ls),
+                       nthreads or os.cpu_count() or 1)
+    return dens, ls
 
 
 def view_render(params: np.ndarray, cam: dict, scaling: float = 1.0, sh_deg: int = 3,

@@ -19,6 +19,7 @@
 
 #include "densify.cuh"
 #include "kernels.cuh"
+#include "knn.cuh"
 #include "plyio.cuh"
 #include "skyfall.h"
 #include "viewer.cuh"
@@ -1309,6 +1310,84 @@ int sky_load_checkpoint(void* p, const char* path) {
   c->scene_extent = h.scene_extent;
   c->densify_runs = h.densify_runs;
   c->prune_runs = h.prune_runs;
+  return SKY_OK;
+}
+
+int sky_knn_init(void* p, float scene_extent, float* density_out) {
+  Context* c = as_ctx(p);
+  if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (c->n == 0) return fail(SKY_ERR_STATE, "no Gaussians loaded");
+  if (c->n >= (1u << 30)) return fail(SKY_ERR_ARG, "k-NN init supports fewer than 2^30 Gaussians");
+  const uint32_t n = c->n;
+  cudaStream_t s = c->stream;
+  const float extent = scene_extent > 0.0f ? scene_extent : c->scene_extent;
+  TempBuf bounds(c), keys(c), ksorted(c), order(c), cstart(c), logs(c), dens(c), smem(c);
+  TRY(dev_alloc(c, bounds.b, 64));
+  uint32_t init[6];
+  for (int k = 0; k < 6; ++k) init[k] = knn_bounds_init(k);
+  CK(cudaMemcpyAsync(bounds.b.p, init, sizeof(init), cudaMemcpyHostToDevice, s));
+  launch_knn_bounds((const float*)c->params.p, c->stride, n, bounds.as<uint32_t>(), s);
+  uint32_t bw[6];
+  CK(cudaMemcpyAsync(bw, bounds.b.p, sizeof(bw), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  // grid: about two points per cell over the bounding box, at most 2^22
+  // cells and 1024 per axis
+  KnnGrid g{};
+  double ext[3], big = 0.0;
+  for (int k = 0; k < 3; ++k) {
+    g.lo[k] = knn_bounds_decode(bw[k]);
+    const float hi = knn_bounds_decode(bw[3 + k]);
+    ext[k] = std::isfinite(g.lo[k]) && std::isfinite(hi) ? std::max(0.0, (double)hi - (double)g.lo[k]) : 0.0;
+    if (!std::isfinite(g.lo[k])) g.lo[k] = 0.0f;
+    big = std::max(big, ext[k]);
+  }
+  double h = big > 0.0 ? big / 1024.0 : 1.0;
+  if (big > 0.0) {
+    const double floor_e = big / 1024.0;
+    const double vol = std::max(ext[0], floor_e) * std::max(ext[1], floor_e) * std::max(ext[2], floor_e);
+    const double want = std::min<double>(std::max<double>(n / 2.0, 1.0), (double)(1u << 22));
+    h = std::max(h, std::cbrt(vol / want));
+  }
+  for (;;) {
+    uint64_t cells = 1;
+    for (int k = 0; k < 3; ++k) {
+      g.dims[k] = (uint32_t)std::min(1024.0, std::max(1.0, std::ceil(ext[k] / h)));
+      cells *= g.dims[k];
+    }
+    if (cells <= (1u << 22)) {
+      g.cells = (uint32_t)cells;
+      break;
+    }
+    h *= 1.25;
+  }
+  g.h = (float)h;
+  TRY(dev_alloc(c, keys.b, (size_t)n * 4));
+  TRY(dev_alloc(c, ksorted.b, (size_t)n * 4));
+  TRY(dev_alloc(c, order.b, (size_t)n * 4));
+  TRY(dev_alloc(c, cstart.b, ((size_t)g.cells + 1) * 4));
+  TRY(dev_alloc(c, logs.b, (size_t)n * 4));
+  if (density_out) TRY(dev_alloc(c, dens.b, (size_t)n * 4));
+  TRY(dev_alloc(c, smem.b, sort_scratch_bytes(n)));
+  launch_knn_keys((const float*)c->params.p, c->stride, n, g, keys.as<uint32_t>(), s);
+  SortScratch sc = sort_scratch_carve(smem.b.p, n);
+  SortSegment seg{nullptr, n};
+  uint32_t* err = bounds.as<uint32_t>() + 8;
+  CK(cudaMemsetAsync(err, 0, 4, s));
+  CK(sort_pairs_launch(keys.as<uint32_t>(), nullptr, ksorted.as<uint32_t>(), order.as<uint32_t>(), seg,
+                       n, std::max<uint32_t>(1, ceil_log2(g.cells)), sc, err, s));
+  launch_knn_cell_ranges(ksorted.as<uint32_t>(), n, g.cells, cstart.as<uint32_t>(), s);
+  launch_knn_query((float*)c->params.p, c->stride, n, g, order.as<uint32_t>(), cstart.as<uint32_t>(),
+                   extent, dens.as<float>(), logs.as<float>(), s);
+  launch_knn_write((float*)c->params.p, c->stride, n, logs.as<float>(), s);
+  c->launches += 10;
+  CK(cudaGetLastError());
+  uint32_t e = 0;
+  CK(cudaMemcpyAsync(&e, err, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  if (e & SKY_DEVERR_SORT_TIMEOUT) return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  if (density_out) CK(cudaMemcpy(density_out, dens.b.p, (size_t)n * 4, cudaMemcpyDeviceToHost));
+  c->fwd_ready = false;
+  c->scores_valid = false;
   return SKY_OK;
 }
 

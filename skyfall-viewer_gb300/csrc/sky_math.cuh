@@ -72,6 +72,41 @@ SKY_DEV float sky_expf(float x) {
   return __uint_as_float(__float_as_uint(p) + (kbits << 23));
 }
 
+// log(x): x = m 2^e with m in [sqrt(1/2), sqrt(2)); log m = 2 atanh(s),
+// s = (m - 1) / (m + 1), |s| <= 0.172, by its odd series to s^11 (Horner in
+// s^2, fused multiply-adds); log x = e ln2 + log m with ln2 split in two.
+// Within 2 ulp of log for positive normal and subnormal x; -inf at 0, NaN
+// below, +inf at +inf.  Written out so that the CPU oracle evaluates the
+// same function bit for bit.
+SKY_DEV float sky_logf(float x) {
+  if (x != x || x < 0.0f) return __int_as_float(0x7FC00000);
+  if (x == 0.0f) return __int_as_float(0xFF800000);
+  if (x == __int_as_float(0x7F800000)) return x;
+  uint32_t b = __float_as_uint(x);
+  int e = 0;
+  if (b < 0x00800000u) {  // subnormal: scale by 2^23
+    x = __fmul_rn(x, 8388608.0f);
+    b = __float_as_uint(x);
+    e = -23;
+  }
+  e += (int)(b >> 23) - 127;
+  float m = __uint_as_float((b & 0x007FFFFFu) | 0x3F800000u);
+  if (m > 1.41421354f) {
+    m = __fmul_rn(m, 0.5f);
+    e += 1;
+  }
+  const float s = __fdiv_rn(__fsub_rn(m, 1.0f), __fadd_rn(m, 1.0f));
+  const float z = __fmul_rn(s, s);
+  float p = 0.181818187f;               // 2/11
+  p = __fmaf_rn(p, z, 0.222222224f);    // 2/9
+  p = __fmaf_rn(p, z, 0.285714298f);    // 2/7
+  p = __fmaf_rn(p, z, 0.400000006f);    // 2/5
+  p = __fmaf_rn(p, z, 0.666666687f);    // 2/3
+  const float lm = __fmaf_rn(__fmul_rn(s, z), p, __fmul_rn(2.0f, s));
+  const float fe = (float)e;
+  return __fmaf_rn(fe, 0.693147182f, __fmaf_rn(fe, -1.90465421e-09f, lm));
+}
+
 SKY_DEV float round_f16(float x) { return __half2float(__float2half_rn(x)); }
 
 // WGSL f32 -> u32: truncation toward zero, saturating; NaN -> 0.

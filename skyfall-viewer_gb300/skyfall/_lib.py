@@ -154,6 +154,7 @@ PROTOTYPES = {
                                 C.POINTER(C.c_double)]),
     "sky_save_checkpoint": (I32, [P, C.c_char_p]),
     "sky_load_checkpoint": (I32, [P, C.c_char_p]),
+    "sky_knn_init": (I32, [P, C.c_float, P]),
     "sky_set_cameras": (I32, [P, C.POINTER(SkyCamera), U32]),
     "sky_set_target": (I32, [P, U32, P, U32, U32]),
     "sky_render": (I32, [P, P, U32, P, P]),

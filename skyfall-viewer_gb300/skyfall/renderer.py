@@ -115,6 +115,13 @@ class GaussianRenderer:
     def savePly(self, path, sh_degree: int = 3) -> None:
         L.check(self._L.sky_save_ply(self._h, str(path).encode(), sh_degree))
 
+    def initializeKnnAndSync(self, scene_extent: float = 0.0) -> np.ndarray:
+        """k-NN scale initialisation; returns the per-Gaussian mean distance
+        to the three nearest neighbours."""
+        d = np.empty(self.getGaussianCount(), np.float32)
+        L.check(self._L.sky_knn_init(self._h, scene_extent, L.ptr(d)))
+        return d
+
     def saveCheckpoint(self, path) -> None:
         L.check(self._L.sky_save_checkpoint(self._h, str(path).encode()))
 

@@ -171,3 +171,24 @@ def test_oracle_exact_adjoint_matches_fp64_finite_differences(orc):
             bad.append((p, i, float(g[p, i]), fd))
     assert checked >= 40
     assert not bad, bad[:5]
+
+
+def test_logf_within_two_ulp(orc):
+    """The oracle's (and the kernels') log: within 2 ulp of the f64 log over
+    normal and subnormal arguments, exact specials."""
+    rng = np.random.default_rng(5)
+    x = np.concatenate([
+        np.exp(rng.uniform(-87, 88, 200000)).astype(np.float32),
+        rng.uniform(0.5, 2.0, 100000).astype(np.float32),
+        (rng.uniform(0, 1, 2000) * 1e-40).astype(np.float32),
+        np.array([1.0, 2.0, 0.5, 1e-6, 0.1, 3.4e38], np.float32),
+    ])
+    x = x[x > 0]
+    got = orc.logf(x).astype(np.float64)
+    want = np.log(x.astype(np.float64))
+    ulp = np.spacing(np.abs(want).astype(np.float32)).astype(np.float64)
+    err = np.abs(got - want) / ulp
+    assert err.max() <= 2.0, err.max()
+    assert orc.logf(np.array([1.0], np.float32))[0] == 0.0
+    sp = orc.logf(np.array([0.0, -1.0, np.inf], np.float32))
+    assert sp[0] == -np.inf and np.isnan(sp[1]) and sp[2] == np.inf
