@@ -357,7 +357,8 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
         float so2 = 0.5f * (s1 + s2);
         so2 = so2 + (r0.w * dx) * dy;
         if (so2 < 0.0f || so2 > r2.y) continue;
-        const float G = sky_expf(-so2);
+        // emitted records have finite means and conics, so 0 <= s <= s_max
+        const float G = sky_expf_inrange(-so2);
         const float al = r1.y * G;
         const float a = fmin_(al, MAX_ALPHA);
         if (a < MIN_ALPHA) continue;
@@ -640,38 +641,40 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
         float so2 = 0.5f * (s1 + s2);
         so2 = so2 + (q0.w * dx) * dy;
         if (so2 >= 0.0f && so2 <= q2.y) {
-          const float G = sky_expf(-so2);
-          const float op = q1.y;
-          const float al = op * G;
+          const float G = sky_expf_inrange(-so2);
+          const float al = q1.y * G;
           const float a = fmin_(al, MAX_ALPHA);
           if (a >= MIN_ALPHA) {
             // The decision above repeats the forward's bit for bit; the
             // gradient arithmetic below only has to be accurate, so it uses
-            // fused multiply-adds and the fast reciprocal division.
+            // fused multiply-adds and the fast reciprocal division.  Per
+            // pair it forms raw moments; the per-splat factors (1 - opacity
+            // for the logit, -1/2 and -1 for the conic, the conic matrix for
+            // the mean) are applied once per splat after the reduction:
+            //   v3 = dL/dalpha * alpha          (dL/dlogit / (1 - opacity))
+            //   g  = dL/dalpha * opacity * G    (= -dL/ds)
+            //   v4..v8 = g dx^2, g dx dy, g dy^2, g dx, g dy.
             contrib = true;
-            const float cr = q1.z, cg = q1.w, cbl = q2.x;
             const float om = fmax_(1.0f - a, 0.0001f);
             const float Tb = __fdividef(T, om);
             const float ctb = a * Tb;
-            const float fg = __fmaf_rn(r2, cbl, __fmaf_rn(r1, cg, r0 * cr));
-            const float bgt = __fmaf_rn(r2, acc2, __fmaf_rn(r1, acc1, r0 * acc0));
-            const float dLda = (fg - bgt) * Tb;
-            const bool live = !(al > MAX_ALPHA);  // the alpha clamp has zero slope
-            const float dlogit = live ? (dLda * a) * (1.0f - op) : 0.0f;
-            const float dLds = live ? -(dLda * op) * G : 0.0f;
-            const float hds = 0.5f * dLds;
+            const float d0 = q1.z - acc0, d1 = q1.w - acc1, d2 = q2.x - acc2;
+            const float dLda = __fmaf_rn(r2, d2, __fmaf_rn(r1, d1, r0 * d0)) * Tb;
+            const float dl = al > MAX_ALPHA ? 0.0f : dLda;  // the alpha clamp has zero slope
+            const float g = dl * al;
+            const float gdx = g * dx, gdy = g * dy;
             val[0] = r0 * ctb;
             val[1] = r1 * ctb;
             val[2] = r2 * ctb;
-            val[3] = dlogit;
-            val[4] = (hds * dx) * dx;
-            val[5] = (dLds * dx) * dy;
-            val[6] = (hds * dy) * dy;
-            val[7] = -dLds * __fmaf_rn(q0.z, dx, q0.w * dy);
-            val[8] = -dLds * __fmaf_rn(q0.w, dx, q1.x * dy);
-            acc0 = __fmaf_rn(a, cr - acc0, acc0);
-            acc1 = __fmaf_rn(a, cg - acc1, acc1);
-            acc2 = __fmaf_rn(a, cbl - acc2, acc2);
+            val[3] = dl * a;
+            val[4] = gdx * dx;
+            val[5] = gdx * dy;
+            val[6] = gdy * dy;
+            val[7] = gdx;
+            val[8] = gdy;
+            acc0 = __fmaf_rn(a, d0, acc0);
+            acc1 = __fmaf_rn(a, d1, acc1);
+            acc2 = __fmaf_rn(a, d2, acc2);
             T = Tb;
           }
         }
@@ -702,10 +705,16 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
 #pragma unroll
         for (int k = 0; k < 9; ++k) sum[k] = sum[k] + s_part[w][j][k];
       }
+      // moments -> dL/dlogit, dL/dconic (a, b, c), dL/dmean (x, y)
+      const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1];
+      const float dlogit = sum[3] * (1.0f - q1.y);
+      const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
+      const float dmx = __fmaf_rn(q0.z, sum[7], q0.w * sum[8]);
+      const float dmy = __fmaf_rn(q0.w, sum[7], q1.x * sum[8]);
       float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
-      dst[0] = make_float4(sum[0], sum[1], sum[2], sum[3]);
-      dst[1] = make_float4(sum[4], sum[5], sum[6], sum[7]);
-      dst[2] = make_float4(sum[8], 0.0f, 0.0f, 0.0f);
+      dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
+      dst[1] = make_float4(dca, dcb, dcc, dmx);
+      dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
     }
   }
 }

@@ -47,10 +47,19 @@ SKY_DEV float clampf_(float x, float lo, float hi) { return fmin_(fmax_(x, lo), 
 // through the exponent field.  Within 1 ulp of exp on [-87, 88]; 0 below,
 // +inf above.  Written out here so that the CPU oracle can evaluate the same
 // function bit for bit.
+SKY_DEV float sky_expf_inrange(float x);
+
 SKY_DEV float sky_expf(float x) {
   if (x != x) return x;
   if (x > 88.0f) return __int_as_float(0x7F800000);
   if (x < -87.0f) return 0.0f;
+  return sky_expf_inrange(x);
+}
+
+// sky_expf without its range checks, for arguments known to lie in
+// [-87, 88] (the rasterizers' -s with 0 <= s <= ln(255) + 1e-3): the same
+// operations, so the same result.
+SKY_DEV float sky_expf_inrange(float x) {
   const float kLog2e = 1.44269502f;
   const float kLn2Hi = 0.693147182f;
   const float kLn2Lo = -1.90465421e-09f;
