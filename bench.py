@@ -56,14 +56,59 @@ def parse():
     ap.add_argument("--no-plain", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-views", type=int, default=1)
-    return ap.parse_args()
+    ap.add_argument("--workload", default="train1080", choices=["train1080", "mixed", "stress4k"],
+                    help="train1080: 1M SH-3 clusters, 16 orbit views 1920x1080 per step; "
+                         "mixed: 16 views per step of 640x480 / 1280x720 / 1920x1080; "
+                         "stress4k: 4M tightly clustered SH-3 Gaussians, one 3840x2160 view")
+    ap.add_argument("--tile-size", type=int, default=16, choices=[8, 16, 32])
+    ap.add_argument("--autotune", action="store_true", help="pick the tile size from 8/16/32 first")
+    args = ap.parse_args()
+    if args.workload == "stress4k":
+        if args.n == 1_000_000:
+            args.n = 4_000_000
+        args.views = args.cameras = 1
+        args.width, args.height = 3840, 2160
+    return args
 
 
 def workload(args):
     from skyfall import scenes
-    P = scenes.scene_clusters(args.n, seed=1002)
-    cams = scenes.cameras_orbit(args.cameras, 5.0, args.width, args.height)
+    if args.workload == "stress4k":
+        P = scenes.scene_clusters(args.n, seed=1005, cluster_sigma=0.05, logscale_mean=-5.0,
+                                  logscale_sigma=0.5)
+    else:
+        P = scenes.scene_clusters(args.n, seed=1002)
+    if args.workload == "mixed":
+        cams = scenes.cameras_mixed(args.cameras, 5.0)
+    else:
+        cams = scenes.cameras_orbit(args.cameras, 5.0, args.width, args.height)
     return P, cams
+
+
+def workload_name(args, n, B, C) -> str:
+    if args.workload == "mixed":
+        return (f"batched train, uneven resolutions: {n} Gaussians SH-3 (64 clusters), {B} views/step "
+                f"from {C} cameras of 640x480 / 1280x720 / 1920x1080, tile {args.tile_size}; "
+                f"1 iteration = 1 view")
+    if args.workload == "stress4k":
+        return (f"memory-stress train: {n} Gaussians SH-3 in 64 clusters of sigma 0.05, log-scales "
+                f"N(-5, 0.5), one 3840x2160 view per step; 1 iteration = 1 view")
+    return (f"batched train: {n} Gaussians SH-3 (64 clusters), {B} views/step of "
+            f"{args.width}x{args.height} from {C} orbit cameras, targets rendered from a "
+            f"{args.gt}-Gaussian scene; 1 iteration = 1 view")
+
+
+def measured_traffic(kernel: str, workload: str):
+    """DRAM bytes per launch of `kernel` on `workload` from an ncu capture
+    recorded in profiles/traffic.json (null when none was taken)."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    d = json.loads(p.read_text())
+    e = d.get(kernel)
+    if not e or e.get("workload") != workload:
+        return None
+    return float(e["bytes_per_launch"])
 
 
 def render_targets(sky, cams, args):
@@ -255,17 +300,26 @@ def main():
 
     P, cams = workload(args)
     targets = render_targets(sky, cams, args)
-    cfg = dict(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0,
-               max_views_per_step=args.views, use_graph=1)
-    r = sky.GaussianRenderer(**cfg)
-    r.load_points(P)
-    r.setTrainingCameras(cams)
-    r.setTrainingImages(targets)
     B = args.views
     C = len(cams)
     rng = np.random.default_rng(1234 + rank)
     batched_sets = [list((np.arange(B) + k * B) % C) for k in range(args.steps)]
     warm_sets = [list(rng.integers(0, C, B)) for _ in range(args.warmup)]
+
+    def make(ts):
+        rr = sky.GaussianRenderer(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2,
+                                  w_ssim=0.0, max_views_per_step=args.views, use_graph=1,
+                                  tile_size=ts)
+        rr.load_points(P)
+        rr.setTrainingCameras(cams)
+        rr.setTrainingImages(targets)
+        return rr
+
+    tune = None
+    if args.autotune:
+        from skyfall.autotune import pick_tile_size
+        args.tile_size, tune = pick_tile_size(make, batched_sets[:3])
+    r = make(args.tile_size)
 
     def barrier():
         if world > 1:
@@ -279,9 +333,11 @@ def main():
     barrier()
     ms = max_over_ranks(res["ms"], world)
     value = replica_throughput(args.steps * B, world, ms)
-    px_per_view = args.width * args.height
+    px_step = [sum(cams[c]["width"] * cams[c]["height"] for c in vs) for vs in batched_sets]
+    px_per_view = sum(px_step) / (len(px_step) * B)
     mpix = value * px_per_view / 1e6
     e2e_value = replica_throughput(args.steps * B, world, max_over_ranks(res["wall"] * 1000.0, world))
+    device_bytes = int(r.getStatus().device_bytes)
 
     plain = None
     plain_stage_ms = None
@@ -304,19 +360,22 @@ def main():
     isect = res["isects"] / steps
     pix = B * px_per_view
     n = args.n
+    # algorithmic bytes per launch (per unit: DESIGN section 3)
     algo_bytes = {
         "preprocess": n * 236 + B * n * 64,
         "scan": B * n * 8,
         "emit": isect * 8 + B * n * 20,
         "sort": isect * 68,
         "ranges": isect * 4,
-        "forward": isect * 64 + pix * 24,
-        "backward": isect * 64 + pix * 28,
-        "geom_adam": n * 1652,
+        "forward": isect * 52 + pix * 60,
+        "backward": isect * 100 + pix * 28,
+        "geom_adam": n * 1652 + isect * 48,
     }
     peak, peak_kind = measured_peak()
     achieved = algo_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
     clocks = clk.summary()
+    wl_key = f"{args.workload}/ts{args.tile_size}"
+    traffic = measured_traffic(dom, wl_key)
 
     cpu = None
     if not args.no_cpu_baseline and rank == 0:
@@ -341,12 +400,12 @@ def main():
         "dtype": "f32",
         "data": "synthetic",
         "config": {
-            "workload": f"batched train: {n} Gaussians SH-3 (64 clusters), {B} views/step of "
-                        f"{args.width}x{args.height} from {C} orbit cameras, targets rendered from a "
-                        f"{args.gt}-Gaussian scene; 1 iteration = 1 view",
+            "workload": workload_name(args, n, B, C),
             "views_per_step": B, "global_batch": B, "parallelism": "replicas" if world > 1 else "none",
+            "tile_size": args.tile_size, "autotune_ms_per_step": tune,
             "l2": "inputs > L2 (no flush)",
         },
+        "device_bytes": device_bytes,
         "mpix_per_s": mpix,
         "plain_iters_per_s": plain,
         "plain_stage_ms": plain_stage_ms,
@@ -359,7 +418,9 @@ def main():
                 "h2d_bytes_per_step": 13312, "d2h_bytes_per_step": 2 * 160},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None},
+                     "traffic": traffic, "algorithmic_bytes": algo_bytes[dom],
+                     "traffic_source": "profiles/traffic.json (ncu dram__bytes_read.sum + "
+                                       "dram__bytes_write.sum, same workload)" if traffic else None},
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

@@ -146,3 +146,22 @@ def test_errors_are_reported(sky):
     assert e.value.code == sky._lib.SKY_ERR_STATE
     with pytest.raises(sky.SkyError):
         r.setTrainingImage(0, np.zeros((16, 16, 3), np.float32))
+
+
+def test_tile_size_autotuner(sky):
+    from skyfall import scenes
+    from skyfall.autotune import pick_tile_size
+    P = scenes.scene_uniform(4096, seed=1501)
+    cams = scenes.cameras_orbit(4, 3.0, 160, 120)
+    tgts = [scenes.target_uniform(160, 120, seed=2500 + k) for k in range(4)]
+
+    def make(ts):
+        r = sky.GaussianRenderer(sh_degree=0, tile_size=ts, use_graph=1, w_ssim=0.0)
+        r.load_points(P)
+        r.setTrainingCameras(cams)
+        r.setTrainingImages(tgts)
+        return r
+
+    best, times = pick_tile_size(make, [[0, 1, 2, 3]] * 3)
+    assert best in (8, 16, 32) and set(times) == {8, 16, 32}
+    assert all(t > 0 for t in times.values()) and times[best] == min(times.values())
