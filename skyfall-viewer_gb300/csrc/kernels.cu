@@ -272,12 +272,12 @@ __global__ void k_ranges_empty(DevBuffers b) {
 // ---------------------------------------------------------------------------
 constexpr int kFwdBatch = 256;
 
-// Bit w set when warp w of the tile (pixel rows [w * 32/TS, (w + 1) * 32/TS))
-// has a pixel centre inside the splat's alpha >= 1/255 bounding box
-// (half-widths r2.z, r2.w around the mean r0.xy; negative = no pixel).
-template <int TS>
+// Bit w set when warp w of the tile (pixel rows [w * RPW, (w + 1) * RPW),
+// RPW = 32/TS unless the warp's lanes hold several pixels) has a pixel centre
+// inside the splat's alpha >= 1/255 bounding box (half-widths r2.z, r2.w
+// around the mean r0.xy; negative = no pixel).
+template <int TS, int RPW = 32 / TS>
 SKY_DEV uint32_t warp_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
-  constexpr int RPW = 32 / TS;
   const float hx = r2.z, hy = r2.w;
   if (!(hx > 0.0f) || !(hy > 0.0f)) return 0u;
   const float cx0 = (float)x0 + 0.5f, cx1 = (float)x0 + ((float)TS - 0.5f);
@@ -706,6 +706,186 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
         for (int k = 0; k < 9; ++k) sum[k] = sum[k] + s_part[w][j][k];
       }
       // moments -> dL/dlogit, dL/dconic (a, b, c), dL/dmean (x, y)
+      const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1];
+      const float dlogit = sum[3] * (1.0f - q1.y);
+      const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
+      const float dmx = __fmaf_rn(q0.z, sum[7], q0.w * sum[8]);
+      const float dmy = __fmaf_rn(q0.w, sum[7], q1.x * sum[8]);
+      float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
+      dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
+      dst[1] = make_float4(dca, dcb, dcc, dmx);
+      dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Backward, exact mode, 16x16 tiles with two pixels per thread: 128 threads,
+// lane l of warp w holds column l % 16 of rows 4w + 2(l / 16) and the row
+// below.  A warp then covers a 16x4 strip; a splat reaches ~0.57 times as
+// many warps as with 16x2 strips, and each (warp, splat) pays its shared
+// loads, list entry and nine-value reduction once for 64 pixels (the two
+// pixels' values are added in the lane first).  Per pixel the arithmetic is
+// that of k_backward_exact; the per-(tile, intersection) sums differ only in
+// summation order.
+// ---------------------------------------------------------------------------
+struct BwdPix {
+  float px, py, T, acc[3], r[3];
+  int hi;
+};
+
+// One (pixel, splat) pair of the exact backward: adds the pair's nine raw
+// moments to val and steps the pixel's transmittance and accumulated colour
+// back past the splat.  Returns whether the splat contributes at the pixel.
+SKY_DEV bool bwd_pair(BwdPix& p, const float4& q0, const float4& q1, const float4& q2, float val[9]) {
+  const float dx = p.px - q0.x, dy = p.py - q0.y;
+  const float s1 = (q0.z * dx) * dx;
+  const float s2 = (q1.x * dy) * dy;
+  float so2 = 0.5f * (s1 + s2);
+  so2 = so2 + (q0.w * dx) * dy;
+  if (!(so2 >= 0.0f && so2 <= q2.y)) return false;
+  const float G = sky_expf_inrange(-so2);
+  const float al = q1.y * G;
+  const float a = fmin_(al, MAX_ALPHA);
+  if (!(a >= MIN_ALPHA)) return false;
+  const float om = fmax_(1.0f - a, 0.0001f);
+  const float Tb = __fdividef(p.T, om);
+  const float ctb = a * Tb;
+  const float d0 = q1.z - p.acc[0], d1 = q1.w - p.acc[1], d2 = q2.x - p.acc[2];
+  const float dLda = __fmaf_rn(p.r[2], d2, __fmaf_rn(p.r[1], d1, p.r[0] * d0)) * Tb;
+  const float dl = al > MAX_ALPHA ? 0.0f : dLda;
+  const float g = dl * al;
+  const float gdx = g * dx, gdy = g * dy;
+  val[0] = __fmaf_rn(p.r[0], ctb, val[0]);
+  val[1] = __fmaf_rn(p.r[1], ctb, val[1]);
+  val[2] = __fmaf_rn(p.r[2], ctb, val[2]);
+  val[3] = __fmaf_rn(dl, a, val[3]);
+  val[4] = __fmaf_rn(gdx, dx, val[4]);
+  val[5] = __fmaf_rn(gdx, dy, val[5]);
+  val[6] = __fmaf_rn(gdy, dy, val[6]);
+  val[7] = val[7] + gdx;
+  val[8] = val[8] + gdy;
+  p.acc[0] = __fmaf_rn(a, d0, p.acc[0]);
+  p.acc[1] = __fmaf_rn(a, d1, p.acc[1]);
+  p.acc[2] = __fmaf_rn(a, d2, p.acc[2]);
+  p.T = Tb;
+  return true;
+}
+
+__global__ void __launch_bounds__(128) k_backward_exact2(DevBuffers b) {
+  constexpr int TS = 16, NT = 128, NW = 4, RPW = 4, kBatch = 64;
+  __shared__ float4 s_rec[kBatch * 3];
+  __shared__ uint32_t s_mask[kBatch];
+  __shared__ float s_part[NW][kBatch][9];
+  __shared__ int s_hi[NW];
+  __shared__ uint8_t s_list[NW][kBatch];
+  const StepParams& sp = *b.sp;
+  const uint32_t tile = blockIdx.x;
+  if (tile >= sp.num_tiles) return;
+  if (capacity_failed(b.status)) return;
+  const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
+  if (start >= end) return;
+  const int v = find_view(sp, tile);
+  const ViewInfo& vi = sp.views[v];
+  const uint32_t local = tile - vi.tile_base;
+  const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t x = tx * TS + (lane & 15u);
+  const uint32_t y0 = ty * TS + warp * RPW + 2u * (lane >> 4);
+  BwdPix pix[2];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    BwdPix& p = pix[h];
+    const uint32_t y = y0 + (uint32_t)h;
+    p.px = (float)x + 0.5f;
+    p.py = (float)y + 0.5f;
+    p.T = 1.0f;
+    p.acc[0] = sp.bg[0]; p.acc[1] = sp.bg[1]; p.acc[2] = sp.bg[2];
+    p.r[0] = p.r[1] = p.r[2] = 0.0f;
+    p.hi = (int)start - 1;
+    if (x < vi.width && y < vi.height) {
+      const size_t q = (size_t)vi.pixel_base + (size_t)y * vi.width + x;
+      const uint32_t lst = b.last[q];
+      if (lst >= start) p.hi = (int)min(lst, end - 1);
+      p.T = b.tfinal[q];
+      const float4 rs = b.residual[q];
+      p.r[0] = rs.x; p.r[1] = rs.y; p.r[2] = rs.z;
+    }
+  }
+  int whi = max(pix[0].hi, pix[1].hi);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) whi = max(whi, __shfl_xor_sync(kFull, whi, o));
+  if (lane == 0) s_hi[warp] = whi;
+  __syncthreads();
+  int hi = s_hi[0];
+  for (int w = 1; w < NW; ++w) hi = max(hi, s_hi[w]);
+  const int slot = scatter9_slot(lane);
+  const uint32_t wbit = 1u << warp;
+  const uint32_t lt = (1u << lane) - 1u;
+  // intersections no pixel reaches get zero partials
+  for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
+    float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
+    dst[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+    dst[1] = make_float4(0.f, 0.f, 0.f, 0.f);
+    dst[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (int bhi = hi; bhi >= (int)start; bhi -= kBatch) {
+    const int cnt = min(kBatch, bhi - (int)start + 1);
+    __syncthreads();
+    for (int k = (int)tid; k < cnt; k += NT) {
+      const size_t r = b.flatten[bhi - k];
+      const float4 q0 = b.records[r * 3 + 0];
+      const float4 q2 = b.records[r * 3 + 2];
+      s_rec[k * 3 + 0] = q0;
+      s_rec[k * 3 + 1] = b.records[r * 3 + 1];
+      s_rec[k * 3 + 2] = q2;
+      s_mask[k] = warp_mask<TS, RPW>(q0, q2, tx * TS, ty * TS);
+    }
+    __syncthreads();
+    uint32_t nlist = 0;
+    for (int base = 0; base < cnt; base += 32) {
+      const int j = base + (int)lane;
+      const bool in = j < cnt && (s_mask[j] & wbit) && bhi - j <= whi;
+      const uint32_t m = __ballot_sync(kFull, in);
+      if (in) s_list[warp][nlist + __popc(m & lt)] = (uint8_t)j;
+      nlist += __popc(m);
+    }
+    __syncwarp();
+    for (uint32_t li = 0; li < nlist; ++li) {
+      const int j = s_list[warp][li];
+      const int i = bhi - j;
+      float val[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) val[k] = 0.0f;
+      const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1], q2 = s_rec[j * 3 + 2];
+      bool contrib = false;
+      if (i <= pix[0].hi) contrib = bwd_pair(pix[0], q0, q1, q2, val);
+      if (i <= pix[1].hi) contrib = bwd_pair(pix[1], q0, q1, q2, val) || contrib;
+      const uint32_t who = __ballot_sync(kFull, contrib);
+      if (who == 0u) {
+        if (slot < 9) s_part[warp][j][slot] = 0.0f;
+      } else if ((who & (who - 1u)) == 0u) {
+        if (contrib) {
+#pragma unroll
+          for (int k = 0; k < 9; ++k) s_part[warp][j][k] = val[k];
+        }
+      } else {
+        const float tot = warp_reduce_scatter9(val, lane);
+        if (slot < 9) s_part[warp][j][slot] = tot;
+      }
+    }
+    __syncthreads();
+    for (int j = (int)tid; j < cnt; j += NT) {
+      const int i = bhi - j;
+      const uint32_t m = s_mask[j];
+      float sum[9];
+#pragma unroll
+      for (int k = 0; k < 9; ++k) sum[k] = 0.0f;
+      for (int w = 0; w < NW; ++w) {
+        if (!((m >> w) & 1u) || i > s_hi[w]) continue;  // warp w skipped this splat
+#pragma unroll
+        for (int k = 0; k < 9; ++k) sum[k] = sum[k] + s_part[w][j][k];
+      }
       const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1];
       const float dlogit = sum[3] * (1.0f - q1.y);
       const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
@@ -1260,7 +1440,7 @@ void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool 
     switch (ts) {
       case 8: k_backward_exact<8><<<max_tiles, 64, 0, s>>>(b); break;
       case 32: k_backward_exact<32><<<max_tiles, 1024, 0, s>>>(b); break;
-      default: k_backward_exact<16><<<max_tiles, 256, 0, s>>>(b); break;
+      default: k_backward_exact2<<<max_tiles, 128, 0, s>>>(b); break;
     }
   } else {
     switch (ts) {
