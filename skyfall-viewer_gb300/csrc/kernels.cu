@@ -276,6 +276,29 @@ constexpr int kFwdBatch = 256;
 // RPW = 32/TS unless the warp's lanes hold several pixels) has a pixel centre
 // inside the splat's alpha >= 1/255 bounding box (half-widths r2.z, r2.w
 // around the mean r0.xy; negative = no pixel).
+// Warps covering BW x BH pixel blocks of the tile, numbered row-major over
+// the TS/BW x TS/BH block grid: bit w set when block w has a pixel centre in
+// the splat's alpha >= 1/255 bounding box.
+template <int TS, int BW, int BH>
+SKY_DEV uint32_t block_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
+  constexpr int NCOL = TS / BW;
+  const float hx = r2.z, hy = r2.w;
+  if (!(hx > 0.0f) || !(hy > 0.0f)) return 0u;
+  const float xlo = r0.x - hx - (float)x0 - 0.5f, xhi = r0.x + hx - (float)x0 - 0.5f;
+  const float ylo = r0.y - hy - (float)y0 - 0.5f, yhi = r0.y + hy - (float)y0 - 0.5f;
+  if (!(xhi >= 0.0f) || !(xlo <= (float)(TS - 1))) return 0u;
+  if (!(yhi >= 0.0f) || !(ylo <= (float)(TS - 1))) return 0u;
+  const int clo = xlo <= 0.0f ? 0 : (int)ceilf(xlo);
+  const int chi = xhi >= (float)(TS - 1) ? TS - 1 : (int)floorf(xhi);
+  const int rlo = ylo <= 0.0f ? 0 : (int)ceilf(ylo);
+  const int rhi = yhi >= (float)(TS - 1) ? TS - 1 : (int)floorf(yhi);
+  if (clo > chi || rlo > rhi) return 0u;
+  const uint32_t cols = ((1u << (chi / BW + 1)) - 1u) & ~((1u << (clo / BW)) - 1u);
+  uint32_t mask = 0u;
+  for (int br = rlo / BH; br <= rhi / BH; ++br) mask |= cols << (br * NCOL);
+  return mask;
+}
+
 template <int TS, int RPW = 32 / TS>
 SKY_DEV uint32_t warp_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
   const float hx = r2.z, hy = r2.w;
@@ -310,7 +333,10 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   const uint32_t local = tile - vi.tile_base;
   const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t x = tx * TS + (tid % TS), y = ty * TS + (tid / TS);
+  // warp w covers the 8x4 pixel block (w % (TS/8), w / (TS/8)) of the tile:
+  // compact blocks meet fewer splats than full-width strips
+  const uint32_t x = tx * TS + 8u * (warp % (TS / 8)) + (lane & 7u);
+  const uint32_t y = ty * TS + 4u * (warp / (TS / 8)) + (lane >> 3);
   const bool inside = x < vi.width && y < vi.height;
   const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
   const float pxf = (float)x + 0.5f, pyf = (float)y + 0.5f;
@@ -331,7 +357,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
       s_rec[k * 3 + 0] = q0;
       s_rec[k * 3 + 1] = b.records[r * 3 + 1];
       s_rec[k * 3 + 2] = q2;
-      s_mask[k] = warp_mask<TS>(q0, q2, tx * TS, ty * TS);
+      s_mask[k] = block_mask<TS, 8, 4>(q0, q2, tx * TS, ty * TS);
     }
     __syncthreads();
     // this warp's splats of the batch, in order (skipped splats cannot pass
@@ -720,14 +746,14 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
 }
 
 // ---------------------------------------------------------------------------
-// Backward, exact mode, 16x16 tiles with two pixels per thread: 128 threads,
-// lane l of warp w holds column l % 16 of rows 4w + 2(l / 16) and the row
-// below.  A warp then covers a 16x4 strip; a splat reaches ~0.57 times as
-// many warps as with 16x2 strips, and each (warp, splat) pays its shared
-// loads, list entry and nine-value reduction once for 64 pixels (the two
-// pixels' values are added in the lane first).  Per pixel the arithmetic is
-// that of k_backward_exact; the per-(tile, intersection) sums differ only in
-// summation order.
+// Backward, exact mode, 16x16 tiles with two pixels per thread: 128 threads;
+// warp w covers the 8x8 block (w & 1, w >> 1) of the tile, lane l holds
+// column l & 7 of block rows 2(l >> 3) and the row below.  A splat reaches
+// about half as many warps as with 16x2 strips, and each (warp, splat) pays
+// its shared loads, list entry and nine-value reduction once for 64 pixels
+// (the two pixels' values are added in the lane first).  Per pixel the
+// arithmetic is that of k_backward_exact; the per-(tile, intersection) sums
+// differ only in summation order.
 // ---------------------------------------------------------------------------
 struct BwdPix {
   float px, py, T, acc[3], r[3];
@@ -773,7 +799,7 @@ SKY_DEV bool bwd_pair(BwdPix& p, const float4& q0, const float4& q1, const float
 }
 
 __global__ void __launch_bounds__(128) k_backward_exact2(DevBuffers b) {
-  constexpr int TS = 16, NT = 128, NW = 4, RPW = 4, kBatch = 64;
+  constexpr int TS = 16, NT = 128, NW = 4, kBatch = 64;
   __shared__ float4 s_rec[kBatch * 3];
   __shared__ uint32_t s_mask[kBatch];
   __shared__ float s_part[NW][kBatch][9];
@@ -790,8 +816,8 @@ __global__ void __launch_bounds__(128) k_backward_exact2(DevBuffers b) {
   const uint32_t local = tile - vi.tile_base;
   const uint32_t tx = local % vi.tiles_x, ty = local / vi.tiles_x;
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const uint32_t x = tx * TS + (lane & 15u);
-  const uint32_t y0 = ty * TS + warp * RPW + 2u * (lane >> 4);
+  const uint32_t x = tx * TS + 8u * (warp & 1u) + (lane & 7u);
+  const uint32_t y0 = ty * TS + 8u * (warp >> 1) + 2u * (lane >> 3);
   BwdPix pix[2];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
@@ -839,7 +865,7 @@ __global__ void __launch_bounds__(128) k_backward_exact2(DevBuffers b) {
       s_rec[k * 3 + 0] = q0;
       s_rec[k * 3 + 1] = b.records[r * 3 + 1];
       s_rec[k * 3 + 2] = q2;
-      s_mask[k] = warp_mask<TS, RPW>(q0, q2, tx * TS, ty * TS);
+      s_mask[k] = block_mask<TS, 8, 8>(q0, q2, tx * TS, ty * TS);
     }
     __syncthreads();
     uint32_t nlist = 0;
