@@ -62,17 +62,55 @@ k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, uint
   const uint32_t lane = threadIdx.x & 31;
   const uint32_t warp_global = (blockIdx.x * kSortThreads + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * kSortThreads) >> 5;
-  // warp-strided chunks of 32 consecutive keys
-  for (uint32_t base = warp_global * 32; base < n; base += nwarps * 32) {
-    uint32_t idx = base + lane;
-    bool valid = idx < n;
-    uint32_t k = valid ? keys[begin + idx] : 0u;
-    uint32_t active = __ballot_sync(0xFFFFFFFFu, valid);
-    if (valid) {
-      for (int p = 0; p < passes; ++p) {
-        uint32_t d = (k >> (8 * p)) & digit_mask(key_bits, p);
-        uint32_t peers = __match_any_sync(active, d);
-        if ((peers & lanemask_lt()) == 0) atomicAdd(&s_hist[p][d], (uint32_t)__popc(peers));
+  const uint32_t above = lane == 31 ? 0u : (0xFFFFFFFFu << (lane + 1));  // lanes after this one
+  // Warp-strided chunks of 128 consecutive keys, 4 per lane (positions
+  // 4 lane .. 4 lane + 3).  Keys arrive in emission order, where neighbours
+  // mostly share their digits (consecutive tiles of one Gaussian), so each
+  // pass counts runs of equal digits: four ballots give every run start of
+  // the chunk, and the key that starts a run adds the run's length (distance
+  // to the next start, or to the chunk's end).
+  for (uint32_t base = warp_global * 128; base < n; base += nwarps * 128) {
+    const uint32_t idx = base + 4 * lane;
+    const uint32_t N = min(128u, n - base);  // valid keys of the chunk (a prefix)
+    const uint32_t nvalid = idx >= n ? 0u : min(4u, n - idx);
+    uint32_t k[4];
+    if (nvalid == 4u && ((begin + idx) & 3u) == 0u) {
+      const uint4 q = *reinterpret_cast<const uint4*>(keys + begin + idx);
+      k[0] = q.x; k[1] = q.y; k[2] = q.z; k[3] = q.w;
+    } else {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) k[j] = (uint32_t)j < nvalid ? keys[begin + idx + j] : 0u;
+    }
+    for (int p = 0; p < passes; ++p) {
+      const uint32_t dm = digit_mask(key_bits, p);
+      uint32_t d[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) d[j] = (k[j] >> (8 * p)) & dm;
+      // a lane with valid keys follows a full lane, so d[3] of lane - 1 is valid
+      const uint32_t prev = __shfl_up_sync(0xFFFFFFFFu, d[3], 1);
+      bool s[4];
+      s[0] = nvalid > 0u && (lane == 0u || d[0] != prev);
+      s[1] = nvalid > 1u && d[1] != d[0];
+      s[2] = nvalid > 2u && d[2] != d[1];
+      s[3] = nvalid > 3u && d[3] != d[2];
+      const uint32_t B0 = __ballot_sync(0xFFFFFFFFu, s[0]), B1 = __ballot_sync(0xFFFFFFFFu, s[1]);
+      const uint32_t B2 = __ballot_sync(0xFFFFFFFFu, s[2]), B3 = __ballot_sync(0xFFFFFFFFu, s[3]);
+      const uint32_t later = (B0 | B1 | B2 | B3) & above;
+      // first run start after this lane's keys
+      uint32_t next_lane_start = N;
+      if (later) {
+        const uint32_t l2 = (uint32_t)__ffs(later) - 1u;
+        const uint32_t j2 = ((B0 >> l2) & 1u) ? 0u : ((B1 >> l2) & 1u) ? 1u : ((B2 >> l2) & 1u) ? 2u : 3u;
+        next_lane_start = 4u * l2 + j2;
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        if (!s[j]) continue;
+        uint32_t next = next_lane_start;
+#pragma unroll
+        for (int jj = 3; jj > j; --jj)
+          if (s[jj]) next = 4u * lane + (uint32_t)jj;
+        atomicAdd(&s_hist[p][d[j]], next - (4u * lane + (uint32_t)j));
       }
     }
   }
