@@ -130,7 +130,7 @@ struct Context {
   Buf flags, flag_scan, d_sp, d_st;
   // densification statistics (float4 per Gaussian) and multi-view scores
   Buf imp_stats, dens_accum, score_imp, score_prune, score_counts, metric_l1, metric_part,
-      metric_stats;
+      metric_stats, item_sums;
   bool scores_valid = false;  // scores belong to (scores_iter, current scene)
   uint64_t scores_iter = 0;
   uint32_t scores_n = 0, scores_views = 0;
@@ -235,6 +235,7 @@ DevBuffers make_buffers(Context* c) {
   b.rec_of = (uint32_t*)c->rec_of.p;
   b.flatten = (uint32_t*)c->flatten.p;
   b.partials = (float4*)c->partials.p;
+  b.item_sums = (float4*)c->item_sums.p;
   b.tile_grads = (int32_t*)c->tile_grads.p;
   b.gsum54 = (long long*)c->gsum54.p;
   b.offsets = (uint32_t*)c->offsets.p;
@@ -351,6 +352,10 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
     if (sh.ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
     launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.ref, s);
     TRY(mark(7));
+    if (!sh.ref) {
+      launch_item_sums(b, items, s);
+      ++launches;
+    }
     launch_geom_adam(b, sh.n, s);
     launches += 2;
   } else {
@@ -460,6 +465,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   if (mode == kBackward) TRY(dev_alloc(c, c->grads, (size_t)kPlanes * c->stride * 4));
   const bool ref = cfg.backward_mode == SKY_BWD_REFERENCE;
   if (ref && mode >= kBackward) TRY(dev_alloc(c, c->gsum54, items * 54 * 8));
+  if (!ref && mode >= kBackward) TRY(dev_alloc(c, c->item_sums, items * 48));
   if (c->icap == 0) TRY(ensure_isect(c, 1u << 16));
   // schedules
   uint64_t it = c->iteration + (mode == kTrain ? 1 : 0);
@@ -1057,7 +1063,7 @@ int sky_destroy(void* p) {
                 &c->metric_part, &c->metric_stats, &c->v_splats, &c->v_keys, &c->v_counts,
                 &c->v_rects, &c->v_order, &c->v_ksorted, &c->v_cum, &c->v_csorted, &c->v_bsums,
                 &c->v_misc, &c->v_tkeys, &c->v_gidx, &c->v_tkeys_s, &c->v_gidx_s, &c->v_offsets,
-                &c->v_rgba, &c->v_sort};
+                &c->v_rgba, &c->v_sort, &c->item_sums};
   for (Buf* b : all) dev_free(c, *b);
   drop_graph(c);
   for (int k = 0; k <= SKY_NUM_STAGES; ++k)

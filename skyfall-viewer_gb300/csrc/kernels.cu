@@ -1259,6 +1259,52 @@ SKY_DEV void adam_elem(float* __restrict__ p, float* __restrict__ m1, float* __r
 
 constexpr int kGeomThreads = 128;
 
+// Exact mode: per (view, Gaussian) item, the sum of its intersections'
+// partials in emission order (pairs added as ((s + a) + c), an odd last one
+// alone), written as 3 float4.  A streaming pass with one thread per item,
+// so the geometry kernel reads one fixed-size record per view instead of a
+// variable-length chain of dependent loads.
+__global__ void __launch_bounds__(256) k_item_sums(DevBuffers b) {
+  const StepParams& sp = *b.sp;
+  if (capacity_failed(b.status)) return;
+  const size_t items = (size_t)sp.num_views * sp.n;
+  for (size_t item = (size_t)blockIdx.x * blockDim.x + threadIdx.x; item < items;
+       item += (size_t)gridDim.x * blockDim.x) {
+    const uint32_t cnt = b.counts[item];
+    if (cnt == 0) continue;  // never read
+    float in9[9];
+#pragma unroll
+    for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
+    const uint32_t e1 = b.cumsum[item], e0 = e1 - cnt;
+    uint32_t e = e0;
+    for (; e + 1 < e1; e += 2) {  // two partials in flight
+      const float4 a0 = b.partials[(size_t)e * 3 + 0];
+      const float4 a1 = b.partials[(size_t)e * 3 + 1];
+      const float4 a2 = b.partials[(size_t)e * 3 + 2];
+      const float4 c0 = b.partials[(size_t)e * 3 + 3];
+      const float4 c1 = b.partials[(size_t)e * 3 + 4];
+      const float4 c2 = b.partials[(size_t)e * 3 + 5];
+      in9[0] = (in9[0] + a0.x) + c0.x; in9[1] = (in9[1] + a0.y) + c0.y;
+      in9[2] = (in9[2] + a0.z) + c0.z; in9[3] = (in9[3] + a0.w) + c0.w;
+      in9[4] = (in9[4] + a1.x) + c1.x; in9[5] = (in9[5] + a1.y) + c1.y;
+      in9[6] = (in9[6] + a1.z) + c1.z; in9[7] = (in9[7] + a1.w) + c1.w;
+      in9[8] = (in9[8] + a2.x) + c2.x;
+    }
+    if (e < e1) {
+      const float4 a0 = b.partials[(size_t)e * 3 + 0];
+      const float4 a1 = b.partials[(size_t)e * 3 + 1];
+      const float4 a2 = b.partials[(size_t)e * 3 + 2];
+      in9[0] = in9[0] + a0.x; in9[1] = in9[1] + a0.y; in9[2] = in9[2] + a0.z;
+      in9[3] = in9[3] + a0.w; in9[4] = in9[4] + a1.x; in9[5] = in9[5] + a1.y;
+      in9[6] = in9[6] + a1.z; in9[7] = in9[7] + a1.w; in9[8] = in9[8] + a2.x;
+    }
+    float4* o = b.item_sums + item * 3;
+    o[0] = make_float4(in9[0], in9[1], in9[2], in9[3]);
+    o[1] = make_float4(in9[4], in9[5], in9[6], in9[7]);
+    o[2] = make_float4(in9[8], 0.0f, 0.0f, 0.0f);
+  }
+}
+
 // SH values and SH-gradient accumulators live in shared memory (one column
 // per thread, conflict-free), which keeps the kernel under 128 registers and
 // four blocks per multiprocessor resident.
@@ -1318,29 +1364,10 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
     bool any = false;
     if (!ref) {
-      const uint32_t e1 = b.cumsum[item], e0 = e1 - cnt;
-      uint32_t e = e0;
-      for (; e + 1 < e1; e += 2) {  // two partials in flight
-        const float4 a0 = b.partials[(size_t)e * 3 + 0];
-        const float4 a1 = b.partials[(size_t)e * 3 + 1];
-        const float4 a2 = b.partials[(size_t)e * 3 + 2];
-        const float4 c0 = b.partials[(size_t)e * 3 + 3];
-        const float4 c1 = b.partials[(size_t)e * 3 + 4];
-        const float4 c2 = b.partials[(size_t)e * 3 + 5];
-        in9[0] = (in9[0] + a0.x) + c0.x; in9[1] = (in9[1] + a0.y) + c0.y;
-        in9[2] = (in9[2] + a0.z) + c0.z; in9[3] = (in9[3] + a0.w) + c0.w;
-        in9[4] = (in9[4] + a1.x) + c1.x; in9[5] = (in9[5] + a1.y) + c1.y;
-        in9[6] = (in9[6] + a1.z) + c1.z; in9[7] = (in9[7] + a1.w) + c1.w;
-        in9[8] = (in9[8] + a2.x) + c2.x;
-      }
-      if (e < e1) {
-        const float4 a0 = b.partials[(size_t)e * 3 + 0];
-        const float4 a1 = b.partials[(size_t)e * 3 + 1];
-        const float4 a2 = b.partials[(size_t)e * 3 + 2];
-        in9[0] = in9[0] + a0.x; in9[1] = in9[1] + a0.y; in9[2] = in9[2] + a0.z;
-        in9[3] = in9[3] + a0.w; in9[4] = in9[4] + a1.x; in9[5] = in9[5] + a1.y;
-        in9[6] = in9[6] + a1.z; in9[7] = in9[7] + a1.w; in9[8] = in9[8] + a2.x;
-      }
+      const float4* s3 = b.item_sums + item * 3;
+      const float4 a0 = s3[0], a1 = s3[1], a2 = s3[2];
+      in9[0] = a0.x; in9[1] = a0.y; in9[2] = a0.z; in9[3] = a0.w;
+      in9[4] = a1.x; in9[5] = a1.y; in9[6] = a1.z; in9[7] = a1.w; in9[8] = a2.x;
 #pragma unroll
       for (int k = 0; k < 9; ++k) any = any || in9[k] != 0.0f;
     } else {
@@ -1480,6 +1507,12 @@ void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool 
 void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s) {
   if (n == 0) return;
   k_geom_adam<<<(n + kGeomThreads - 1) / kGeomThreads, kGeomThreads, 0, s>>>(b);
+}
+
+void launch_item_sums(const DevBuffers& b, uint64_t items, cudaStream_t s) {
+  if (items == 0) return;
+  const uint64_t blocks = std::min<uint64_t>((items + 255) / 256, (uint64_t)sm_count() * 16);
+  k_item_sums<<<(uint32_t)blocks, 256, 0, s>>>(b);
 }
 
 }  // namespace sky

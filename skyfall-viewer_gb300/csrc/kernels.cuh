@@ -18,6 +18,8 @@ void launch_loss_final(const DevBuffers& b, cudaStream_t s);
 void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ref,
                      cudaStream_t s);
 void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s);
+// Exact mode, before launch_geom_adam: per-item sums of the partials.
+void launch_item_sums(const DevBuffers& b, uint64_t items, cudaStream_t s);
 
 // Prune / densify / opacity reset (compact.cu).
 void launch_prune_flags(const float* params, uint32_t stride, uint32_t n, float min_opacity,

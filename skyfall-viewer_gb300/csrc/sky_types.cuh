@@ -83,6 +83,7 @@ struct DevBuffers {
   uint32_t* rec_of;       // item per emitted intersection
   uint32_t* flatten;      // item per sorted intersection
   float4* partials;       // 3 float4 per intersection (emission order)
+  float4* item_sums;      // exact mode: 3 float4 per item, its partials summed
   int32_t* tile_grads;    // reference mode: 54 per sorted intersection
   long long* gsum54;      // reference mode: 54 per item
   uint32_t* offsets;      // tile ranges, num_tiles + 1
