@@ -760,9 +760,22 @@ struct BwdPix {
   int hi;
 };
 
+// exp(-s) for 0 <= s <= ln(255) + 1e-3 by the ex2.approx instruction
+// (relative error below 1e-6 here, including the rounding of -s log2 e).
+SKY_DEV float exp_neg_approx(float s) {
+  float r;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s * -1.44269504f));
+  return r;
+}
+
 // One (pixel, splat) pair of the exact backward: adds the pair's nine raw
 // moments to val and steps the pixel's transmittance and accumulated colour
 // back past the splat.  Returns whether the splat contributes at the pixel.
+// Which pairs contribute (alpha >= 1/255) and which are clamped (alpha >
+// 0.999) must be decided exactly as the forward decided them; the gradient
+// values only have to be accurate.  So alpha comes from the fast exponential,
+// and from sky_expf (the forward's) only when it lies within 2e-6 relative of
+// either threshold, where the two could decide differently.
 SKY_DEV bool bwd_pair(BwdPix& p, const float4& q0, const float4& q1, const float4& q2, float val[9]) {
   const float dx = p.px - q0.x, dy = p.py - q0.y;
   const float s1 = (q0.z * dx) * dx;
@@ -770,8 +783,12 @@ SKY_DEV bool bwd_pair(BwdPix& p, const float4& q0, const float4& q1, const float
   float so2 = 0.5f * (s1 + s2);
   so2 = so2 + (q0.w * dx) * dy;
   if (!(so2 >= 0.0f && so2 <= q2.y)) return false;
-  const float G = sky_expf_inrange(-so2);
-  const float al = q1.y * G;
+  float G = exp_neg_approx(so2);
+  float al = q1.y * G;
+  if (fabsf(al - MIN_ALPHA) <= 2e-6f * MIN_ALPHA || fabsf(al - MAX_ALPHA) <= 2e-6f) {
+    G = sky_expf_inrange(-so2);
+    al = q1.y * G;
+  }
   const float a = fmin_(al, MAX_ALPHA);
   if (!(a >= MIN_ALPHA)) return false;
   const float om = fmax_(1.0f - a, 0.0001f);
@@ -798,7 +815,7 @@ SKY_DEV bool bwd_pair(BwdPix& p, const float4& q0, const float4& q1, const float
   return true;
 }
 
-__global__ void __launch_bounds__(128) k_backward_exact2(DevBuffers b) {
+__global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   constexpr int TS = 16, NT = 128, NW = 4, kBatch = 64;
   __shared__ float4 s_rec[kBatch * 3];
   __shared__ uint32_t s_mask[kBatch];
