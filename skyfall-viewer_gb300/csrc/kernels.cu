@@ -1362,9 +1362,20 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     imp = reinterpret_cast<const float4*>(b.importance)[g];
     acc = reinterpret_cast<const float4*>(b.densify_accum)[g];
   }
+  // the next view's tile count is loaded one iteration ahead, so its latency
+  // hides behind the current view's adjoint
+  uint32_t cnt_next = b.counts[g];
   for (uint32_t v = 0; v < sp.num_views; ++v) {
     const size_t item = (size_t)v * sp.n + g;
-    const uint32_t cnt = b.counts[item];
+    const uint32_t cnt = cnt_next;
+    if (v + 1 < sp.num_views) cnt_next = b.counts[item + sp.n];
+    float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0;
+    if (cnt > 0u && !ref) {
+      const float4* s3 = b.item_sums + item * 3;
+      a0 = s3[0];
+      a1 = s3[1];
+      a2 = s3[2];
+    }
     if (stats) {
       imp.x = imp.x * sp.importance_decay;
       imp.y = imp.y * sp.importance_decay;
@@ -1381,8 +1392,6 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
     bool any = false;
     if (!ref) {
-      const float4* s3 = b.item_sums + item * 3;
-      const float4 a0 = s3[0], a1 = s3[1], a2 = s3[2];
       in9[0] = a0.x; in9[1] = a0.y; in9[2] = a0.z; in9[3] = a0.w;
       in9[4] = a1.x; in9[5] = a1.y; in9[6] = a1.z; in9[7] = a1.w; in9[8] = a2.x;
 #pragma unroll
