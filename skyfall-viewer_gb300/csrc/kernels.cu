@@ -776,12 +776,14 @@ SKY_DEV float exp_neg_approx(float s) {
 // values only have to be accurate.  So alpha comes from the fast exponential,
 // and from sky_expf (the forward's) only when it lies within 2e-6 relative of
 // either threshold, where the two could decide differently.
-SKY_DEV bool bwd_pair(BwdPix& p, const float4& q0, const float4& q1, const float4& q2, float val[9]) {
-  const float dx = p.px - q0.x, dy = p.py - q0.y;
-  const float s1 = (q0.z * dx) * dx;
+// dx = px - mx, s1 = (a dx) dx and bdx = b dx belong to the pixel column and
+// are shared by the lane's two pixels.
+SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0, const float4& q1,
+                      const float4& q2, float val[9]) {
+  const float dy = p.py - q0.y;
   const float s2 = (q1.x * dy) * dy;
   float so2 = 0.5f * (s1 + s2);
-  so2 = so2 + (q0.w * dx) * dy;
+  so2 = so2 + bdx * dy;
   if (!(so2 >= 0.0f && so2 <= q2.y)) return false;
   float G = exp_neg_approx(so2);
   float al = q1.y * G;
@@ -901,9 +903,11 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
 #pragma unroll
       for (int k = 0; k < 9; ++k) val[k] = 0.0f;
       const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1], q2 = s_rec[j * 3 + 2];
+      const float dx = pix[0].px - q0.x;
+      const float s1 = (q0.z * dx) * dx, bdx = q0.w * dx;
       bool contrib = false;
-      if (i <= pix[0].hi) contrib = bwd_pair(pix[0], q0, q1, q2, val);
-      if (i <= pix[1].hi) contrib = bwd_pair(pix[1], q0, q1, q2, val) || contrib;
+      if (i <= pix[0].hi) contrib = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, val);
+      if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val) || contrib;
       const uint32_t who = __ballot_sync(kFull, contrib);
       if (who == 0u) {
         if (slot < 9) s_part[warp][j][slot] = 0.0f;
