@@ -818,7 +818,7 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
 }
 
 __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
-  constexpr int TS = 16, NT = 128, NW = 4, kBatch = 64;
+  constexpr int TS = 16, NT = 128, NW = 4, kBatch = 128;
   __shared__ float4 s_rec[kBatch * 3];
   __shared__ uint32_t s_mask[kBatch];
   __shared__ float s_part[NW][kBatch][9];
