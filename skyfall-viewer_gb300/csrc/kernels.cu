@@ -35,8 +35,13 @@ SKY_DEV bool capacity_failed(const DevStatus* st) {
   return *(volatile const uint32_t*)&st->error != 0u;
 }
 
-// Writes the raster record, depth/radius, tile count and rectangle of one item.
-SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, size_t item) {
+// Raster pre-filter bound of a Gaussian with this opacity (see write_projection).
+SKY_DEV float alpha_skip_bound(float opacity) { return __logf(255.0f * opacity) + 1e-3f; }
+
+// Writes the raster record, depth/radius, tile count and rectangle of one
+// item; smax_g = alpha_skip_bound(o.opacity), the same for every view.
+SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, float smax_g,
+                              size_t item) {
   // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
   // whatever the rounding of exp (|error| < 1e-6 << 1e-3), so skipping it
   // there decides as the reference does.  The pixels with s <= smax lie in
@@ -47,7 +52,7 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, si
   // 1.25 smax + 0.01: no pixel it excludes can pass the alpha test.
   float smax = -1.0f, hx = -1.0f, hy = -1.0f;
   if (ok) {
-    smax = __logf(255.0f * o.opacity) + 1e-3f;
+    smax = smax_g;
     if (smax > 0.0f) {
       const float sb = 2.0f * (1.25f * smax + 0.01f);
       hx = sqrtf(sb * o.cov00) + 0.01f;
@@ -80,12 +85,16 @@ __global__ void __launch_bounds__(256) k_preprocess(DevBuffers b) {
   for (int k = 0; k < kPlanes; ++k)
     prm[k] = (k < 11 + nsh) ? load_plane(b.params, stride, k, g, r16) : 0.0f;
   auto get = [&](int plane) { return prm[plane]; };
+  // the covariance, opacity and skip bound do not depend on the view
+  GaussCov3 gc;
+  gauss_cov3(get, gc);
+  const float smax_g = alpha_skip_bound(gc.opacity);
   for (uint32_t v = 0; v < sp.num_views; ++v) {
     const ViewInfo& vi = sp.views[v];
     ProjOut o;
-    const bool ok = project_gaussian(get, vi, sp, deg, true, o);
+    const bool ok = project_gaussian(get, gc, vi, sp, deg, true, o);
     const size_t item = (size_t)v * sp.n + g;
-    write_projection(b, o, ok, item);
+    write_projection(b, o, ok, smax_g, item);
   }
 }
 
@@ -1114,46 +1123,30 @@ struct Grad11 {
   float pos[3], ls[3], q[4], logit;
 };
 
-SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& sp,
-                        const float* prm /*11 geometry params*/, const float in9[9],
-                        bool color_dir, const float* sh /*48 values at sh[k * sh_stride]*/,
-                        int sh_stride, int deg, Grad11& gr) {
+// One view of the adjoint, up to the 3D covariance: adds the view's dL/dmean
+// and dL/dlogit to gr and its dL/dC3 to g3 (the symmetric V^T GW V, entries
+// 00 01 02 11 12 22).  The chain from C3 to the scales and the quaternion is
+// linear in dL/dC3, so it runs once per Gaussian on the sum over views
+// (geom_cov_final).  pc is the camera-space mean, o.dir / o.raw the view
+// direction and the unclamped SH colour.
+SKY_DEV void geom_view(const float pc[4], const ProjOut& o, const ViewInfo& vi, const StepParams& sp,
+                       const float (&C3)[3][3], const float in9[9], bool color_dir,
+                       const float* sh /*48 values at sh[k * sh_stride]*/, int sh_stride, int deg,
+                       Grad11& gr, float g3[6]) {
   // mean -> camera space
   float dpc[3] = {0.f, 0.f, 0.f};
   float clip[4];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) clip[r] = mat4_row(vi.proj, r, o.pc[0], o.pc[1], o.pc[2], o.pc[3]);
-  const float ndx = clip[0] / clip[3], ndy = clip[1] / clip[3];
-  const float hW = 0.5f * (float)vi.width, hH = 0.5f * (float)vi.height;
+  for (int r = 0; r < 4; ++r) clip[r] = mat4_row(vi.proj, r, pc[0], pc[1], pc[2], pc[3]);
+  const float rw = 1.0f / clip[3];
+  const float ndx = clip[0] * rw, ndy = clip[1] * rw;
+  const float gx = in9[7] * (0.5f * (float)vi.width) * rw, gy = in9[8] * (0.5f * (float)vi.height) * rw;
 #pragma unroll
   for (int j = 0; j < 3; ++j) {
-    dpc[j] += in9[7] * hW * (vi.proj[j * 4 + 0] - ndx * vi.proj[j * 4 + 3]) / clip[3];
-    dpc[j] += in9[8] * hH * (vi.proj[j * 4 + 1] - ndy * vi.proj[j * 4 + 3]) / clip[3];
+    dpc[j] += gx * (vi.proj[j * 4 + 0] - ndx * vi.proj[j * 4 + 3]);
+    dpc[j] += gy * (vi.proj[j * 4 + 1] - ndy * vi.proj[j * 4 + 3]);
   }
   // covariance
-  float sig[3], lsg[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    const float raw = prm[3 + k];
-    sig[k] = expf(clampf_(raw, -10.0f, 10.0f));
-    lsg[k] = (raw > -10.0f && raw < 10.0f) ? 1.0f : 0.0f;
-  }
-  const float qr0 = prm[6], qr1 = prm[7], qr2 = prm[8], qr3 = prm[9];
-  const float ql = sqrtf(qr0 * qr0 + qr1 * qr1 + qr2 * qr2 + qr3 * qr3);
-  const float x = qr0 / ql, y = qr1 / ql, z = qr2 / ql, w = qr3 / ql;
-  float R[3][3] = {{1.f - 2.f * (y * y + z * z), 2.f * (x * y - w * z), 2.f * (x * z + w * y)},
-                   {2.f * (x * y + w * z), 1.f - 2.f * (x * x + z * z), 2.f * (y * z - w * x)},
-                   {2.f * (x * z - w * y), 2.f * (y * z + w * x), 1.f - 2.f * (x * x + y * y)}};
-  float M[3][3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) M[a][c] = R[a][c] * sig[c];
-  float C3[3][3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) C3[a][c] = M[a][0] * M[c][0] + M[a][1] * M[c][1] + M[a][2] * M[c][2];
   float V3[3][3];  // math rows
 #pragma unroll
   for (int r = 0; r < 3; ++r)
@@ -1168,7 +1161,7 @@ SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& 
   for (int a = 0; a < 2; ++a)
 #pragma unroll
     for (int c = 0; c < 2; ++c) Wm[a][c] = tmp[a][0] * V3[c][0] + tmp[a][1] * V3[c][1] + tmp[a][2] * V3[c][2];
-  const float tz = o.pc[2];
+  const float tz = pc[2];
   const float kx = vi.focal[0] / tz, ky = vi.focal[1] / tz;
   const float C00 = kx * kx * Wm[0][0], C01 = kx * ky * Wm[0][1], C11 = ky * ky * Wm[1][1];
   const float e00 = C00 + sp.eps2d, e11 = C11 + sp.eps2d;
@@ -1186,37 +1179,19 @@ SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& 
   const float dW00 = dC00 * kx * kx, dW01 = dC01 * kx * ky, dW11 = dC11 * ky * ky;
   dpc[2] += -2.0f / tz * (dC00 * C00 + dC01 * C01 + dC11 * C11);
   // G3 = V3^T GW V3 with GW = [[dW00, dW01/2, 0], [dW01/2, dW11, 0], [0, 0, 0]]
-  float G3[3][3];
+  const float hW01 = 0.5f * dW01;
+  float u0[3], u1[3];  // GW V3, rows 0 and 1
 #pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int c = 0; c < 3; ++c)
-      G3[a][c] = V3[0][a] * (dW00 * V3[0][c] + 0.5f * dW01 * V3[1][c]) +
-                 V3[1][a] * (0.5f * dW01 * V3[0][c] + dW11 * V3[1][c]);
-  float dR[3][3], dsig[3] = {0.f, 0.f, 0.f};
-#pragma unroll
-  for (int a = 0; a < 3; ++a)
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const float dM = 2.0f * (G3[a][0] * M[0][c] + G3[a][1] * M[1][c] + G3[a][2] * M[2][c]);
-      dR[a][c] = dM * sig[c];
-      dsig[c] += dM * R[a][c];
-    }
-  float dq[4];
-  dq[0] = 2 * y * (dR[0][1] + dR[1][0]) + 2 * z * (dR[0][2] + dR[2][0]) +
-          2 * w * (dR[2][1] - dR[1][2]) - 4 * x * (dR[1][1] + dR[2][2]);
-  dq[1] = -4 * y * (dR[0][0] + dR[2][2]) + 2 * x * (dR[0][1] + dR[1][0]) +
-          2 * w * (dR[0][2] - dR[2][0]) + 2 * z * (dR[1][2] + dR[2][1]);
-  dq[2] = -4 * z * (dR[0][0] + dR[1][1]) + 2 * w * (dR[1][0] - dR[0][1]) +
-          2 * x * (dR[0][2] + dR[2][0]) + 2 * y * (dR[1][2] + dR[2][1]);
-  dq[3] = -2 * z * dR[0][1] + 2 * y * dR[0][2] + 2 * z * dR[1][0] - 2 * x * dR[1][2] -
-          2 * y * dR[2][0] + 2 * x * dR[2][1];
-  const float qd = x * dq[0] + y * dq[1] + z * dq[2] + w * dq[3];
-  const float qn[4] = {x, y, z, w};
-#pragma unroll
-  for (int k = 0; k < 4; ++k) gr.q[k] += (dq[k] - qn[k] * qd) / ql;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) gr.ls[k] += dsig[k] * sig[k] * lsg[k];
+  for (int c = 0; c < 3; ++c) {
+    u0[c] = dW00 * V3[0][c] + hW01 * V3[1][c];
+    u1[c] = hW01 * V3[0][c] + dW11 * V3[1][c];
+  }
+  g3[0] += V3[0][0] * u0[0] + V3[1][0] * u1[0];
+  g3[1] += V3[0][0] * u0[1] + V3[1][0] * u1[1];
+  g3[2] += V3[0][0] * u0[2] + V3[1][0] * u1[2];
+  g3[3] += V3[0][1] * u0[1] + V3[1][1] * u1[1];
+  g3[4] += V3[0][1] * u0[2] + V3[1][1] * u1[2];
+  g3[5] += V3[0][2] * u0[2] + V3[1][2] * u1[2];
   gr.logit += in9[3];
   // colour -> view direction
   if (color_dir && deg > 0 && sh) {
@@ -1252,7 +1227,7 @@ SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& 
       addk(14, SH_C3_5 * 2.f * X * Z, SH_C3_5 * (-2.f * Yv * Z), SH_C3_5 * (xx - yy));
       addk(15, SH_C3_6 * (3.f * xx - 3.f * yy), SH_C3_6 * (-6.f * X * Yv), 0.f);
     }
-    float vl = sqrtf(o.pc[0] * o.pc[0] + o.pc[1] * o.pc[1] + o.pc[2] * o.pc[2]);
+    float vl = sqrtf(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
     const float dd = X * ddir[0] + Yv * ddir[1] + Z * ddir[2];
     dpc[0] += -(ddir[0] - X * dd) / vl;
     dpc[1] += -(ddir[1] - Yv * dd) / vl;
@@ -1260,6 +1235,47 @@ SKY_DEV void geom_chain(const ProjOut& o, const ViewInfo& vi, const StepParams& 
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) gr.pos[j] += V3[0][j] * dpc[0] + V3[1][j] * dpc[1] + V3[2][j] * dpc[2];
+}
+
+// dL/dC3 summed over the views (g3, entries 00 01 02 11 12 22) through
+// C3 = M M^T, M = R diag(sigma), to log sigma (zero slope where the clamp to
+// [-10, 10] is active) and the quaternion (through the normalisation).
+SKY_DEV void geom_cov_final(const float* prm /*11 geometry params*/, const float g3[6], Grad11& gr) {
+  float sig[3], lsg[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const float raw = prm[3 + k];
+    sig[k] = sky_expf(clampf_(raw, -10.0f, 10.0f));
+    lsg[k] = (raw > -10.0f && raw < 10.0f) ? 1.0f : 0.0f;
+  }
+  float R[3][3], qn[4], ql;
+  gauss_rotation([&](int plane) { return prm[plane]; }, R, qn, ql);
+  const float x = qn[0], y = qn[1], z = qn[2], w = qn[3];
+  const float G3[3][3] = {{g3[0], g3[1], g3[2]}, {g3[1], g3[3], g3[4]}, {g3[2], g3[4], g3[5]}};
+  float dR[3][3], dsig[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+  for (int a = 0; a < 3; ++a)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      // dL/dM = 2 G3 M
+      const float dM = 2.0f * sig[c] * (G3[a][0] * R[0][c] + G3[a][1] * R[1][c] + G3[a][2] * R[2][c]);
+      dR[a][c] = dM * sig[c];
+      dsig[c] += dM * R[a][c];
+    }
+  float dq[4];
+  dq[0] = 2 * y * (dR[0][1] + dR[1][0]) + 2 * z * (dR[0][2] + dR[2][0]) +
+          2 * w * (dR[2][1] - dR[1][2]) - 4 * x * (dR[1][1] + dR[2][2]);
+  dq[1] = -4 * y * (dR[0][0] + dR[2][2]) + 2 * x * (dR[0][1] + dR[1][0]) +
+          2 * w * (dR[0][2] - dR[2][0]) + 2 * z * (dR[1][2] + dR[2][1]);
+  dq[2] = -4 * z * (dR[0][0] + dR[1][1]) + 2 * w * (dR[1][0] - dR[0][1]) +
+          2 * x * (dR[0][2] + dR[2][0]) + 2 * y * (dR[1][2] + dR[2][1]);
+  dq[3] = -2 * z * dR[0][1] + 2 * y * dR[0][2] + 2 * z * dR[1][0] - 2 * x * dR[1][2] -
+          2 * y * dR[2][0] + 2 * x * dR[2][1];
+  const float qd = x * dq[0] + y * dq[1] + z * dq[2] + w * dq[3];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) gr.q[k] += (dq[k] - qn[k] * qd) / ql;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) gr.ls[k] += dsig[k] * sig[k] * lsg[k];
 }
 
 SKY_DEV void adam_elem(float* __restrict__ p, float* __restrict__ m1, float* __restrict__ m2,
@@ -1357,6 +1373,9 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   for (int k = 0; k < 4; ++k) gr.q[k] = 0.f;
   gr.logit = 0.f;
   auto get = [&](int plane) { return plane < 11 ? prm[plane] : s_sh[plane - 11][t]; };
+  GaussCov3 gc;
+  gauss_cov3(get, gc);
+  float g3[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};  // dL/dC3 summed over the views
   // Densification statistics of training steps, per view in view order:
   // importance-accum.wgsl:19-40 (decayed tile count, visibility, screen
   // radius) and densify-accum.wgsl:19-46 (|dL/dmean2d|, |dL/dconic|, count).
@@ -1426,10 +1445,15 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
       }
     }
     if (!any) continue;
+    // an item with tiles passed the preprocess's culling with these same
+    // parameters, so only the camera-space mean, the view direction and the
+    // colour are formed again
     const ViewInfo& vi = sp.views[v];
+    float pc[4];
+    view_position(get, vi, pc);
     ProjOut o;
-    if (!project_gaussian(get, vi, sp, deg, !ref, o)) continue;
-    geom_chain(o, vi, sp, prm, in9, !ref, &s_sh[0][t], kGeomThreads, deg, gr);
+    view_color(get, pc, deg, !ref, o);
+    geom_view(pc, o, vi, sp, gc.C3, in9, !ref, &s_sh[0][t], kGeomThreads, deg, gr, g3);
     if (need_sh_grads && !ref) {
       float Y[16];
       sh_basis(o.dir[0], o.dir[1], o.dir[2], deg, Y);
@@ -1446,6 +1470,7 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     reinterpret_cast<float4*>(b.importance)[g] = imp;
     reinterpret_cast<float4*>(b.densify_accum)[g] = acc;
   }
+  geom_cov_final(prm, g3, gr);
   float g11[11] = {gr.pos[0], gr.pos[1], gr.pos[2], gr.ls[0], gr.ls[1], gr.ls[2],
                    gr.q[0],   gr.q[1],   gr.q[2],   gr.q[3],  gr.logit};
   if (sp.write_grads) {

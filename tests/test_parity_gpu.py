@@ -200,7 +200,16 @@ def test_batched_gradients_are_sum_of_per_view(sky):
         r.forward([v])
         per.append(r.backward())
     expect = (per[0] + per[1]) + per[2]
-    assert np.array_equal(gb, expect)
+    # position (0-2), logit (10) and SH (11-58) are added per view in view
+    # order: exactly the sum
+    exact = np.r_[0:3, 10:59]
+    assert np.array_equal(gb[exact], expect[exact])
+    # log sigma (3-5) and the quaternion (6-9) come from one pass of the
+    # covariance chain over dL/dC3 summed across the views, the per-view runs
+    # from one pass each: equal up to f32 rounding of the linear chain
+    cov = np.r_[3:10]
+    scale = max(float(np.abs(p[cov]).max()) for p in per)
+    assert np.max(np.abs(gb[cov] - expect[cov])) <= 1e-5 * scale
 
 
 def test_gradients_are_deterministic(sky):
