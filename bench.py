@@ -360,7 +360,9 @@ def main():
     isect = res["isects"] / steps
     pix = B * px_per_view
     n = args.n
-    # algorithmic bytes per launch (per unit: DESIGN section 3)
+    # algorithmic bytes per launch: per-unit figures x units.  Backward per
+    # intersection: the 48-byte record, its 4-byte item index and the 48-byte
+    # partial; per pixel: last index, transmittance, residual.
     algo_bytes = {
         "preprocess": n * 236 + B * n * 64,
         "scan": B * n * 8,
