@@ -227,8 +227,11 @@ typedef struct SkySchedule {
                                   mean x, y, conic a, b, c, opacity, colour r,
                                   g, b, alpha-skip bound on s, box half-widths */
 #define SKY_BUF_COUNTS 2       /* per (view, Gaussian) tile count, u32            */
-#define SKY_BUF_CUMSUM 3       /* inclusive scan of the counts, u32               */
+#define SKY_BUF_CUMSUM 3       /* inclusive scan of the counts taken in emission
+                                  order (SKY_BUF_ITEM_ORDER), u32                 */
 #define SKY_BUF_KEYS_EMIT 4    /* keys in emission order, u32                     */
+#define SKY_BUF_ITEM_ORDER 20  /* (view, Gaussian) item at each emission position:
+                                  items by (view, depth16, Gaussian), u32        */
 #define SKY_BUF_KEYS_SORTED 5  /* keys after the sort, u32                        */
 #define SKY_BUF_VALS_SORTED 6  /* emission index after the sort, u32              */
 #define SKY_BUF_FLATTEN 7      /* record index per sorted intersection, u32       */

@@ -431,7 +431,7 @@ uint32_t tiles_w(const Cam& c, const Settings& s) { return (c.width + s.tile_siz
 uint32_t tiles_h(const Cam& c, const Settings& s) { return (c.height + s.tile_size - 1) / s.tile_size; }
 
 // Key of one intersection: (tile << 16) | u32(clamp(depth, 0, 65535)) & 0xFFFF.
-// encode_isect_key (training-tiles.wgsl:257-263) with camera 0 and a tile
+// encode_isect_key (training-tiles.wgsl:192-198) with camera 0 and a tile
 // field wide enough for the view (identical to the 12-bit field when the
 // view has at most 4096 tiles).
 uint32_t isect_key(uint32_t tile, float depth) {

@@ -125,6 +125,9 @@ struct Context {
   uint32_t n = 0, stride = 0;
   Buf params, m1, m2, grads, tmp_planes;
   Buf records, aux, counts, rects, cumsum, block_sums;
+  // item order (view, depth16, Gaussian): sort keys, sorted keys, permutation
+  Buf ikeys, ikeys_sorted, perm, item_end, isort_mem;
+  SortScratch isort{};
   Buf keys, keys_sorted, vals_sorted, rec_of, flatten, partials, tile_grads, gsum54;
   Buf offsets, loss_partials, color, alpha, tfinal, last, residual, targets, sort_mem;
   Buf flags, flag_scan, d_sp, d_st;
@@ -227,6 +230,10 @@ DevBuffers make_buffers(Context* c) {
   b.aux = (float2*)c->aux.p;
   b.counts = (uint32_t*)c->counts.p;
   b.rects = (uint2*)c->rects.p;
+  b.ikeys = (uint32_t*)c->ikeys.p;
+  b.perm = (uint32_t*)c->perm.p;
+  b.ikeys_sorted = (uint32_t*)c->ikeys_sorted.p;
+  b.item_end = (uint32_t*)c->item_end.p;
   b.cumsum = (uint32_t*)c->cumsum.p;
   b.block_sums = (uint32_t*)c->block_sums.p;
   b.keys = (uint32_t*)c->keys.p;
@@ -312,9 +319,23 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
   launches = 0;
   CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
+  DevStatus* dst = (DevStatus*)c->d_st.p;
   TRY(mark(0));
   launch_preprocess(b, sh.n, sh.nv, s);
   TRY(mark(1));
+  // Emission order of the items: per sort group (its items are contiguous),
+  // a stable sort by depth16.  Emitting in this order lets the intersection
+  // sort skip the two depth digits.
+  {
+    const StepParams* d_sp = (const StepParams*)c->d_sp.p;
+    for (uint32_t g = 0; g < sh.ngroups; ++g) {
+      // bounds = {item_begin, item_end} of the group, in device memory
+      SortSegment seg{&d_sp->groups[g].item_begin, 0};
+      CK(sort_pairs_launch(b.ikeys, nullptr, (uint32_t*)c->ikeys_sorted.p, b.perm, seg,
+                           (uint32_t)items, 16, c->isort, &dst->error, s));
+      launches += 4;
+    }
+  }
   launch_scan(b, (uint32_t)items, s);
   launch_group_bounds(b, s);
   launches += 5;
@@ -334,12 +355,13 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
   TRY(mark(2));
   launch_emit(b, sh.n, sh.nv, s);
   TRY(mark(3));
-  DevStatus* dst = (DevStatus*)c->d_st.p;
   for (uint32_t g = 0; g < sh.ngroups; ++g) {
+    // keys were emitted in depth order within each tile's items: sorting on
+    // the tile field (digits 2 and 3) alone gives the full key order
     SortSegment seg{&dst->group_bounds[g][0], 0};
     CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap, sh.key_bits[g],
-                         c->sort, &dst->error, s));
-    launches += 2 + (sh.key_bits[g] + 7) / 8;
+                         c->sort, &dst->error, s, 2));
+    launches += 2 + (sh.key_bits[g] + 7) / 8 - 2;
   }
   TRY(mark(4));
   launch_ranges(b, c->icap, s);
@@ -454,6 +476,12 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   TRY(dev_alloc(c, c->counts, items * 4));
   TRY(dev_alloc(c, c->rects, items * 8));
   TRY(dev_alloc(c, c->cumsum, items * 4));
+  TRY(dev_alloc(c, c->ikeys, items * 4));
+  TRY(dev_alloc(c, c->ikeys_sorted, items * 4));
+  TRY(dev_alloc(c, c->perm, items * 4));
+  TRY(dev_alloc(c, c->item_end, items * 4));
+  TRY(dev_alloc(c, c->isort_mem, sort_scratch_bytes((uint32_t)items)));
+  c->isort = sort_scratch_carve(c->isort_mem.p, (uint32_t)items);
   TRY(dev_alloc(c, c->block_sums, (scan_block_count((uint32_t)items) + 1) * 4));
   TRY(dev_alloc(c, c->offsets, (tile_cap + 1) * 4));
   TRY(dev_alloc(c, c->loss_partials, (tile_cap + 1) * 8));
@@ -1054,7 +1082,8 @@ int sky_destroy(void* p) {
   if (!c) return SKY_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records, &c->aux,
-                &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->keys,
+                &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->ikeys,
+                &c->ikeys_sorted, &c->perm, &c->item_end, &c->isort_mem, &c->keys,
                 &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->partials,
                 &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
@@ -1561,6 +1590,7 @@ int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* siz
     case SKY_BUF_DEPTH_RADIUS: src = c->aux.p; sz = items * 8; break;
     case SKY_BUF_COUNTS: src = c->counts.p; sz = items * 4; break;
     case SKY_BUF_CUMSUM: src = c->cumsum.p; sz = items * 4; break;
+    case SKY_BUF_ITEM_ORDER: src = c->perm.p; sz = items * 4; break;
     case SKY_BUF_KEYS_EMIT: src = c->keys.p; sz = I * 4; break;
     case SKY_BUF_KEYS_SORTED: src = c->keys_sorted.p; sz = I * 4; break;
     case SKY_BUF_VALS_SORTED: src = c->vals_sorted.p; sz = I * 4; break;

@@ -38,10 +38,18 @@ SKY_DEV bool capacity_failed(const DevStatus* st) {
 // Raster pre-filter bound of a Gaussian with this opacity (see write_projection).
 SKY_DEV float alpha_skip_bound(float opacity) { return __logf(255.0f * opacity) + 1e-3f; }
 
-// Writes the raster record, depth/radius, tile count and rectangle of one
-// item; smax_g = alpha_skip_bound(o.opacity), the same for every view.
+// The depth field of an intersection key: u32(clamp(depth, 0, 65535)) & 0xFFFF
+// (encode_isect_key, training-tiles.wgsl:192-198).
+SKY_DEV uint32_t depth_key(float depth) {
+  return wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
+}
+
+// Writes the raster record, depth/radius, tile count, rectangle and item sort
+// key (view << 16) | depth16 of one item of view `view` (the sort orders by
+// the depth field; the view rides along for the emission);
+// smax_g = alpha_skip_bound(o.opacity), the same for every view.
 SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, float smax_g,
-                              size_t item) {
+                              uint32_t view, size_t item) {
   // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
   // whatever the rounding of exp (|error| < 1e-6 << 1e-3), so skipping it
   // there decides as the reference does.  The pixels with s <= smax lie in
@@ -66,6 +74,7 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
   b.aux[item] = make_float2(o.depth, o.radius);
   b.counts[item] = o.count;
   b.rects[item] = make_uint2(o.x0 | (o.y0 << 16), o.x1 | (o.y1 << 16));
+  b.ikeys[item] = (view << 16) | depth_key(o.depth);
 }
 
 // ---------------------------------------------------------------------------
@@ -96,7 +105,7 @@ __global__ void __launch_bounds__(256, 3) k_preprocess(DevBuffers b) {
     ProjOut o;
     const bool ok = project_gaussian(get, gc, vi, sp, deg, true, o);
     const size_t item = (size_t)v * sp.n + g;
-    write_projection(b, o, ok, smax_g, item);
+    write_projection(b, o, ok, smax_g, v, item);
   }
 }
 
@@ -128,13 +137,19 @@ SKY_DEV uint32_t block_excl_scan(uint32_t x, uint32_t* s_warp, uint32_t& total) 
   return y - x + add;
 }
 
+// Count at scan position i: the counts are scanned in perm order when a
+// permutation is given.
+SKY_DEV uint32_t scan_count(const DevBuffers& b, uint32_t i) {
+  return b.counts[b.perm ? b.perm[i] : i];
+}
+
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevBuffers b, uint32_t n_items) {
   __shared__ uint32_t s_warp[kScanThreads / 32];
   const uint32_t base = blockIdx.x * kScanTile;
   uint32_t sum = 0;
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t i = base + k * kScanThreads + threadIdx.x;
-    if (i < n_items) sum += b.counts[i];
+    if (i < n_items) sum += scan_count(b, i);
   }
   uint32_t total;
   block_excl_scan(sum, s_warp, total);
@@ -162,7 +177,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint3
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t i = base + k;
-    v[k] = i < n_items ? b.counts[i] : 0u;
+    v[k] = i < n_items ? scan_count(b, i) : 0u;
     sum += v[k];
   }
   uint32_t total;
@@ -171,7 +186,10 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint3
   for (int k = 0; k < kScanItems; ++k) {
     run += v[k];
     uint32_t i = base + k;
-    if (i < n_items) b.cumsum[i] = run;
+    if (i < n_items) {
+      b.cumsum[i] = run;
+      if (b.perm) b.item_end[b.perm[i]] = run;
+    }
   }
 }
 
@@ -194,27 +212,42 @@ __global__ void k_group_bounds(DevBuffers b) {
 }
 
 // ---------------------------------------------------------------------------
-// Key emission: (key_tile << 16) | depth16 in row-major tile order per item,
-// items in (view, Gaussian) order -- emit_intersections
-// (training-tiles.wgsl:265-311) with a per-group tile field.
+// Key emission: (key_tile << 16) | depth16 in row-major tile order per item
+// -- emit_intersections (training-tiles.wgsl:265-311) with a per-group tile
+// field.  Items are emitted in perm order -- per sort group, by depth16, ties
+// in (view, Gaussian) order -- not in (view, Gaussian) order.  A tile belongs
+// to one view, so a stable sort of these keys on the tile field alone yields
+// the order of the reference's stable sort of the full keys over (view,
+// Gaussian) emission: within a tile by depth16, ties by Gaussian.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const StepParams& sp = *b.sp;
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t v = blockIdx.y;
   if (g >= sp.n || v >= sp.num_views) return;
-  const size_t item = (size_t)v * sp.n + g;
-  const uint32_t cnt = b.counts[item];
-  if (cnt == 0) return;
-  const uint32_t end = b.cumsum[item];
-  if (end > sp.icap) return;
-  uint32_t cur = end - cnt;
-  const ViewInfo& vi = sp.views[v];
+  const uint32_t pos = v * sp.n + g;  // position in emission (perm) order
+  // items of one sort group's views interleave: the sorted item key carries
+  // the item's own view and its depth field
+  uint32_t item, view, dq;
+  if (b.perm) {
+    item = b.perm[pos];
+    const uint32_t ik = b.ikeys_sorted[pos];
+    view = ik >> 16;
+    dq = ik & 0xFFFFu;
+  } else {
+    item = pos;
+    view = v;
+    dq = depth_key(b.aux[item].x);
+  }
   const uint2 rc = b.rects[item];
   const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
-  const float depth = b.aux[item].x;
-  const uint32_t dq = wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
-  const uint32_t it = (uint32_t)item;
+  if (x1 <= x0 || y1 <= y0) return;  // no tiles (the count is the rectangle's area)
+  const uint32_t cnt = (x1 - x0) * (y1 - y0);
+  const uint32_t end = b.cumsum[pos];
+  if (end > sp.icap) return;
+  uint32_t cur = end - cnt;
+  const ViewInfo& vi = sp.views[view];
+  const uint32_t it = item;
   for (uint32_t ty = y0; ty < y1; ++ty)
     for (uint32_t tx = x0; tx < x1; ++tx) {
       const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
@@ -1314,7 +1347,7 @@ __global__ void __launch_bounds__(256) k_item_sums(DevBuffers b) {
     float in9[9];
 #pragma unroll
     for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
-    const uint32_t e1 = b.cumsum[item], e0 = e1 - cnt;
+    const uint32_t e1 = b.perm ? b.item_end[item] : b.cumsum[item], e0 = e1 - cnt;
     uint32_t e = e0;
     for (; e + 1 < e1; e += 2) {  // two partials in flight
       const float4 a0 = b.partials[(size_t)e * 3 + 0];

@@ -75,7 +75,12 @@ struct DevBuffers {
   float2* aux;        // depth, radius per item
   uint32_t* counts;   // tiles per item
   uint2* rects;       // packed tile rectangle per item
-  uint32_t* cumsum;   // inclusive scan of counts
+  uint32_t* ikeys;    // per item (view << 16) | depth16; sorted on depth16 per group
+  uint32_t* ikeys_sorted;  // the item keys in emission (perm) order
+  uint32_t* perm;     // item at each emission position: by (group, depth16, item)
+                      // (NULL: item order)
+  uint32_t* cumsum;   // inclusive scan of counts, in perm order
+  uint32_t* item_end; // per item, the end of its emitted range (cumsum at its position)
   uint32_t* block_sums;
   uint32_t* keys;         // emission order
   uint32_t* keys_sorted;

@@ -45,8 +45,9 @@ __device__ __forceinline__ void seg_bounds(const SortSegment& s, uint32_t& b, ui
 // Digit counts of every pass in one read of the keys; also clears the
 // look-back words of the tiles this segment will use.
 __global__ void __launch_bounds__(kSortThreads)
-k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, uint32_t key_bits,
-            uint32_t* __restrict__ hist, uint32_t* __restrict__ lookback, uint32_t max_tiles) {
+k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, int digit_lo,
+            uint32_t key_bits, uint32_t* __restrict__ hist, uint32_t* __restrict__ lookback,
+            uint32_t max_tiles) {
   __shared__ uint32_t s_hist[kMaxPasses][kRadix];
   for (int i = threadIdx.x; i < kMaxPasses * kRadix; i += kSortThreads) (&s_hist[0][0])[i] = 0;
   uint32_t begin, n;
@@ -81,7 +82,7 @@ k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, uint
 #pragma unroll
       for (int j = 0; j < 4; ++j) k[j] = (uint32_t)j < nvalid ? keys[begin + idx + j] : 0u;
     }
-    for (int p = 0; p < passes; ++p) {
+    for (int p = digit_lo; p < passes; ++p) {
       const uint32_t dm = digit_mask(key_bits, p);
       uint32_t d[4];
 #pragma unroll
@@ -125,14 +126,15 @@ k_sort_hist(const uint32_t* __restrict__ keys, SortSegment seg, int passes, uint
 // trivial[pass] = 1 when one digit holds every key (the pass would be the
 // identity permutation, e.g. the high byte of the integer depth).
 __global__ void __launch_bounds__(kRadix)
-k_sort_scan(uint32_t* __restrict__ hist, SortSegment seg, uint32_t* __restrict__ trivial) {
+k_sort_scan(uint32_t* __restrict__ hist, SortSegment seg, uint32_t* __restrict__ trivial,
+            int digit_lo) {
   __shared__ uint32_t s_warp[kRadix / 32];
   uint32_t begin, n;
   seg_bounds(seg, begin, n);
   uint32_t* h = hist + blockIdx.x * kRadix;
   uint32_t v = h[threadIdx.x];
   const int one_digit = __syncthreads_or(v == n);
-  if (threadIdx.x == 0) trivial[blockIdx.x] = one_digit ? 1u : 0u;
+  if (threadIdx.x == 0) trivial[blockIdx.x] = (one_digit || (int)blockIdx.x < digit_lo) ? 1u : 0u;
   uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   uint32_t x = v;
 #pragma unroll
@@ -150,7 +152,7 @@ k_sort_scan(uint32_t* __restrict__ hist, SortSegment seg, uint32_t* __restrict__
 __global__ void __launch_bounds__(kSortThreads)
 k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_dst_out,
            uint32_t* vals_dst_out, uint32_t* keys_tmp, uint32_t* vals_tmp, SortSegment seg,
-           int pass, int passes, const uint32_t* __restrict__ trivial, uint32_t key_bits,
+           int pass, int passes, int digit_lo, const uint32_t* __restrict__ trivial, uint32_t key_bits,
            const uint32_t* __restrict__ hist, uint32_t* __restrict__ tile_counter,
            uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err) {
   __shared__ uint32_t s_keys[kSortTile];
@@ -161,9 +163,10 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
   __shared__ uint32_t s_scan[kWarps];
   __shared__ uint32_t s_tile;
 
-  // Trivial passes are skipped; the m remaining passes alternate between the
-  // temporary and the output buffers so that the last one writes the output
-  // (with m == 0, pass 0 runs anyway and copies).
+  // Trivial passes (and those below digit_lo, which are not launched) are
+  // skipped; the m remaining passes alternate between the temporary and the
+  // output buffers so that the last one writes the output (with m == 0, pass
+  // digit_lo runs anyway and copies: its digit is the same for every key).
   int m = 0, j = 0;
   bool skip = false;
   for (int p = 0; p < passes; ++p) {
@@ -175,7 +178,7 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
     if (p == pass) skip = t;
   }
   if (m == 0) {
-    if (pass != 0) return;
+    if (pass != digit_lo) return;
     skip = false;
     m = 1;
   }
@@ -355,10 +358,11 @@ SortScratch sort_scratch_carve(void* base, uint32_t max_n) {
 cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
-                              uint32_t* err, cudaStream_t stream) {
+                              uint32_t* err, cudaStream_t stream, int digit_lo) {
   if (key_bits == 0) key_bits = 1;
   if (key_bits > 32) key_bits = 32;
   const int passes = (int)((key_bits + 7) / 8);
+  digit_lo = std::max(0, std::min(digit_lo, passes - 1));
   cudaError_t e = cudaMemsetAsync(sc.hist, 0, kMaxPasses * kRadix * 4, stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(sc.tile_counter, 0, 256, stream);
@@ -366,16 +370,16 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
   uint32_t tiles = (max_n + kSortTile - 1) / kSortTile;
   if (tiles == 0) tiles = 1;
   uint32_t hist_blocks = tiles < 1024u ? tiles : 1024u;
-  k_sort_hist<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, seg, passes, key_bits, sc.hist,
-                                                         sc.lookback, sc.max_tiles);
+  k_sort_hist<<<hist_blocks, kSortThreads, 0, stream>>>(keys_in, seg, passes, digit_lo, key_bits,
+                                                         sc.hist, sc.lookback, sc.max_tiles);
   uint32_t* trivial = sc.tile_counter + 8;  // cleared with the tile tickets above
-  k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist, seg, trivial);
-  for (int p = 0; p < passes; ++p)
+  k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist, seg, trivial, digit_lo);
+  for (int p = digit_lo; p < passes; ++p)
     k_onesweep<<<std::min<uint32_t>(tiles, (uint32_t)sm_count() * 4), kSortThreads, 0,
                  stream>>>(keys_in, vals_in, keys_out, vals_out,
                                                     sc.keys_tmp, sc.vals_tmp, seg, p, passes,
-                                                    trivial, key_bits, sc.hist, sc.tile_counter,
-                                                    sc.lookback, sc.max_tiles, err);
+                                                    digit_lo, trivial, key_bits, sc.hist,
+                                                    sc.tile_counter, sc.lookback, sc.max_tiles, err);
   return cudaGetLastError();
 }
 

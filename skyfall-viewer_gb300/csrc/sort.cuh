@@ -44,13 +44,16 @@ struct SortSegment {
 };
 
 // Launch the full sort on `stream`.  keys_in/vals_in: input (vals_in may be
-// NULL, meaning value = position relative to the segment start); results in
+// NULL, meaning value = the key's position in keys_in); results in
 // keys_out/vals_out at the same positions.  key_bits: 1..32.  err: device
 // word receiving error bits.  max_n: bound on the segment size (grid size).
+// digit_lo: 8-bit digits below it are not sorted on -- for keys whose input
+// order is already ascending in those bits among equal higher bits, the
+// result is the full sort.
 cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
-                              uint32_t* err, cudaStream_t stream);
+                              uint32_t* err, cudaStream_t stream, int digit_lo = 0);
 
 // Multiprocessors of the current device (cached per device).
 int sm_count();

@@ -33,14 +33,14 @@ SKY_BWD_REFERENCE = 1
 BUF = dict(
     records=1, counts=2, cumsum=3, keys_emit=4, keys_sorted=5, vals_sorted=6, flatten=7,
     tile_offsets=8, color=9, alpha=10, last_ids=11, residual=12, partials=13, tile_grads=14,
-    grads=15, groups=16, step_scalars=17, depth_radius=18, view_rgba=19,
+    grads=15, groups=16, step_scalars=17, depth_radius=18, view_rgba=19, item_order=20,
 )
 BUF_DTYPE = dict(
     records=np.float32, counts=np.uint32, cumsum=np.uint32, keys_emit=np.uint32,
     keys_sorted=np.uint32, vals_sorted=np.uint32, flatten=np.uint32, tile_offsets=np.uint32,
     color=np.float32, alpha=np.float32, last_ids=np.uint32, residual=np.float32,
     partials=np.float32, tile_grads=np.int32, grads=np.float32, groups=np.uint32,
-    step_scalars=np.float32, depth_radius=np.float32, view_rgba=np.float32,
+    step_scalars=np.float32, depth_radius=np.float32, view_rgba=np.float32, item_order=np.uint32,
 )
 
 ERROR_NAMES = {

@@ -85,16 +85,19 @@ def test_small_view_forward_bit_exact(sky, orc):
 
 def per_gaussian_partials(r, n, items_base=0):
     """Sums the GPU per-intersection partials per (view, Gaussian) item, in
-    float64, using the emission-order ranges of the cumsum."""
+    float64, using the emission-order ranges of the cumsum (items are emitted
+    in the order of the item_order buffer)."""
     part = r.read_buffer("partials").reshape(-1, 12)[:, :9].astype(np.float64)
     counts = r.read_buffer("counts").astype(np.int64)
     cum = r.read_buffer("cumsum").astype(np.int64)
+    order = r.read_buffer("item_order").astype(np.int64)
     items = counts.shape[0]
+    assert np.array_equal(np.sort(order), np.arange(items))
+    emitted = counts[order]                      # counts in emission order
+    assert np.array_equal(np.cumsum(emitted), cum)
     out = np.zeros((items, 9))
-    starts = cum - counts
-    nz = np.nonzero(counts)[0]
-    seg_id = np.repeat(np.arange(items), counts)
-    np.add.at(out, seg_id, part[: cum[-1]])
+    seg_item = np.repeat(order, emitted)          # item of every emitted intersection
+    np.add.at(out, seg_item, part[: cum[-1]])
     return out
 
 
@@ -176,7 +179,7 @@ def test_batched_views_match_per_view_oracle_sh3(sky, orc):
     r.forward(views)
     s = oracle_settings(orc, cfg)
     rgba = r.read_buffer("color").reshape(-1, 4)
-    cum = r.read_buffer("cumsum")
+    counts = r.read_buffer("counts").astype(np.int64)
     tile_base = isect_base = pix = 0
     for k, v in enumerate(views):
         ref = orc.view_pipeline(P, cams[v], tgt[v], s, 3, mode=0)
@@ -186,7 +189,9 @@ def test_batched_views_match_per_view_oracle_sh3(sky, orc):
         assert np.array_equal(rgba[pix:pix + npx], ref["fw"]["rgba"])
         tw, th = orc.tiles_wh(cams[v], 16)
         tile_base += tw * th
-        isect_base = int(cum[(k + 1) * n - 1])
+        # sorted by tile, a view's intersections follow those of the views
+        # before it in the sort group (emission interleaves them by depth)
+        isect_base += int(counts[k * n:(k + 1) * n].sum())
         pix += npx
 
 
