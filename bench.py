@@ -367,7 +367,7 @@ def main():
         "preprocess": n * 236 + B * n * 64,
         "scan": B * n * 8,
         "emit": isect * 8 + B * n * 20,
-        "sort": isect * 68,
+        "sort": isect * 36,
         "ranges": isect * 4,
         "forward": isect * 52 + pix * 60,
         "backward": isect * 100 + pix * 28,
