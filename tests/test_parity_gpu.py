@@ -195,6 +195,49 @@ def test_batched_views_match_per_view_oracle_sh3(sky, orc):
         pix += npx
 
 
+def test_two_sort_groups_match_per_view_oracle(sky, orc):
+    """Three 1920x1080 views at 8-pixel tiles: 32,400 tiles each, so the
+    step splits into two sort groups (views 0-1 and view 2; a group holds at
+    most 65,536 tiles).  Items are emitted per group in depth order and the
+    intersections sorted on the tile field only: keys, tile ranges, item
+    lists and images must still be those of the oracle's per-view full-key
+    sort, and the per-item partial sums its gradients."""
+    P = scenes.scene_clusters(20000, seed=1011, clusters=16, center_range=1.0, cluster_sigma=0.25,
+                              logscale_mean=-3.8)
+    cams = scenes.cameras_orbit(3, 3.5, 1920, 1080)
+    tgt = [scenes.target_uniform(1920, 1080, seed=2200 + k) for k in range(3)]
+    cfg = dict(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0, tile_size=8)
+    n = P.shape[1]
+    r = make(sky, P, cams, tgt, **cfg)
+    r.forward([0, 1, 2])
+    groups = r.read_buffer("groups").reshape(-1, 2)
+    assert groups.shape[0] == 2
+    s = oracle_settings(orc, cfg)
+    rgba = r.read_buffer("color").reshape(-1, 4)
+    counts = r.read_buffer("counts").astype(np.int64)
+    tw, th = orc.tiles_wh(cams[0], 8)
+    tile_base = isect_base = pix = 0
+    refs = []
+    for k in range(3):
+        ref = orc.view_pipeline(P, cams[k], tgt[k], s, 3, mode=0)
+        refs.append(ref)
+        ref["group_tile_base"] = 0 if k < 2 else 2 * tw * th
+        if k == 2:
+            assert isect_base == int(groups[1, 0])
+        check_view(r, ref, n, k, tile_base, k * n, isect_base)
+        npx = 1920 * 1080
+        assert np.array_equal(rgba[pix:pix + npx], ref["fw"]["rgba"])
+        tile_base += tw * th
+        isect_base += int(counts[k * n:(k + 1) * n].sum())
+        pix += npx
+    assert isect_base == int(groups[1, 1])
+    r.backward()
+    gpu9 = per_gaussian_partials(r, n)
+    for k in range(3):
+        ref9, mass = refs[k]["bw"]["gsum9"], refs[k]["bw"]["gabs9"]
+        assert np.all(np.abs(gpu9[k * n:(k + 1) * n] - ref9) <= 2e-5 * mass + 1e-9)
+
+
 def test_batched_gradients_are_sum_of_per_view(sky):
     P, cams, tgt, cfg = clustered_case(8000)
     r = make(sky, P, cams, tgt, **cfg)
