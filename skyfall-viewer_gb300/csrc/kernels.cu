@@ -1377,12 +1377,37 @@ __global__ void __launch_bounds__(256) k_item_sums(DevBuffers b) {
   }
 }
 
+// Asynchronous 16-byte global -> shared copy through L2, and its group fences.
+SKY_DEV void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+SKY_DEV void cp_async8(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+SKY_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+SKY_DEV void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+
+// Dynamic shared memory of k_geom_adam: SH values and SH-gradient
+// accumulators (48 x threads f32 each), two buffers of the threads' item
+// sums (3 float4 per thread) and two of their (depth, radius) pairs.
+constexpr size_t kGeomSmem =
+    (size_t)96 * kGeomThreads * 4 + (size_t)2 * 3 * kGeomThreads * 16 + (size_t)2 * kGeomThreads * 8;
+
 // SH values and SH-gradient accumulators live in shared memory (one column
-// per thread, conflict-free), which keeps the kernel under 128 registers and
-// four blocks per multiprocessor resident.
+// per thread, conflict-free), as do the item sums of the next view, copied
+// asynchronously while the current view's adjoint runs; three blocks per
+// multiprocessor resident (168 registers, 60 KB of shared memory each).
 __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
-  __shared__ float s_sh[48][kGeomThreads];
-  __shared__ float s_gsh[48][kGeomThreads];
+  extern __shared__ float4 s_dyn[];
+  float* const s_base = reinterpret_cast<float*>(s_dyn);
+  float (*s_sh)[kGeomThreads] = reinterpret_cast<float (*)[kGeomThreads]>(s_base);
+  float (*s_gsh)[kGeomThreads] = reinterpret_cast<float (*)[kGeomThreads]>(s_base + 48 * kGeomThreads);
+  float4 (*s_is)[3][kGeomThreads] =
+      reinterpret_cast<float4 (*)[3][kGeomThreads]>(s_base + 96 * kGeomThreads);
+  float2 (*s_aux)[kGeomThreads] =
+      reinterpret_cast<float2 (*)[kGeomThreads]>(s_base + 96 * kGeomThreads + 2 * 3 * kGeomThreads * 4);
   const StepParams& sp = *b.sp;
   if (capacity_failed(b.status)) return;
   const int t = threadIdx.x;
@@ -1420,19 +1445,36 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     imp = reinterpret_cast<const float4*>(b.importance)[g];
     acc = reinterpret_cast<const float4*>(b.densify_accum)[g];
   }
-  // the next view's tile count is loaded one iteration ahead, so its latency
-  // hides behind the current view's adjoint
+  // The next view's tile count is loaded one iteration ahead and its item
+  // sums are copied into shared memory, so their latency hides behind the
+  // current view's adjoint.  Each thread copies and reads only its own column
+  // (no block barrier); a copy of an item with no tiles is never read.
+  auto stage = [&](uint32_t v, int buf) {
+    const size_t it = (size_t)v * sp.n + g;
+    if (!ref) {
+      const float4* src = b.item_sums + it * 3;
+      cp_async16(&s_is[buf][0][t], src + 0);
+      cp_async16(&s_is[buf][1][t], src + 1);
+      cp_async16(&s_is[buf][2][t], src + 2);
+    }
+    if (stats) cp_async8(&s_aux[buf][t], b.aux + it);
+  };
+  stage(0, 0);
+  cp_async_commit();
   uint32_t cnt_next = b.counts[g];
   for (uint32_t v = 0; v < sp.num_views; ++v) {
     const size_t item = (size_t)v * sp.n + g;
+    const int buf = (int)(v & 1u);
+    if (v + 1 < sp.num_views) stage(v + 1, buf ^ 1);
+    cp_async_commit();
+    cp_async_wait1();  // every group but the newest is complete: view v's copy
     const uint32_t cnt = cnt_next;
     if (v + 1 < sp.num_views) cnt_next = b.counts[item + sp.n];
     float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0;
     if (cnt > 0u && !ref) {
-      const float4* s3 = b.item_sums + item * 3;
-      a0 = s3[0];
-      a1 = s3[1];
-      a2 = s3[2];
+      a0 = s_is[buf][0][t];
+      a1 = s_is[buf][1][t];
+      a2 = s_is[buf][2][t];
     }
     if (stats) {
       imp.x = imp.x * sp.importance_decay;
@@ -1441,7 +1483,7 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
       if (cnt > 0u) {
         imp.x = imp.x + (float)cnt;
         imp.y = imp.y + 1.0f;
-        imp.z = fmax_(imp.z, b.aux[item].y);
+        imp.z = fmax_(imp.z, s_aux[buf][t].y);
       }
     }
     if (cnt == 0) continue;
@@ -1596,7 +1638,14 @@ void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool 
 
 void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s) {
   if (n == 0) return;
-  k_geom_adam<<<(n + kGeomThreads - 1) / kGeomThreads, kGeomThreads, 0, s>>>(b);
+  static bool smem_set[64] = {};  // per device: the opt-in above 48 KB
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
+  if (!smem_set[dev]) {
+    cudaFuncSetAttribute(k_geom_adam, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGeomSmem);
+    smem_set[dev] = true;
+  }
+  k_geom_adam<<<(n + kGeomThreads - 1) / kGeomThreads, kGeomThreads, kGeomSmem, s>>>(b);
 }
 
 void launch_item_sums(const DevBuffers& b, uint64_t items, cudaStream_t s) {
