@@ -45,11 +45,11 @@ SKY_DEV uint32_t depth_key(float depth) {
 }
 
 // Writes the raster record, depth/radius, tile count, rectangle and item sort
-// key (view << 16) | depth16 of one item of view `view` (the sort orders by
-// the depth field; the view rides along for the emission);
+// key (min(count, 0xFFFF) << 16) | depth16 of one item (the sort orders by the
+// depth field; the count rides along for the scan in emission order);
 // smax_g = alpha_skip_bound(o.opacity), the same for every view.
 SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, float smax_g,
-                              uint32_t view, size_t item) {
+                              size_t item) {
   // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
   // whatever the rounding of exp (|error| < 1e-6 << 1e-3), so skipping it
   // there decides as the reference does.  The pixels with s <= smax lie in
@@ -74,7 +74,7 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
   b.aux[item] = make_float2(o.depth, o.radius);
   b.counts[item] = o.count;
   b.rects[item] = make_uint2(o.x0 | (o.y0 << 16), o.x1 | (o.y1 << 16));
-  b.ikeys[item] = (view << 16) | depth_key(o.depth);
+  b.ikeys[item] = (min(o.count, 0xFFFFu) << 16) | depth_key(o.depth);
 }
 
 // ---------------------------------------------------------------------------
@@ -105,7 +105,7 @@ __global__ void __launch_bounds__(256, 3) k_preprocess(DevBuffers b) {
     ProjOut o;
     const bool ok = project_gaussian(get, gc, vi, sp, deg, true, o);
     const size_t item = (size_t)v * sp.n + g;
-    write_projection(b, o, ok, smax_g, v, item);
+    write_projection(b, o, ok, smax_g, item);
   }
 }
 
@@ -138,9 +138,12 @@ SKY_DEV uint32_t block_excl_scan(uint32_t x, uint32_t* s_warp, uint32_t& total) 
 }
 
 // Count at scan position i: the counts are scanned in perm order when a
-// permutation is given.
+// permutation is given, read from the sorted item keys (which carry them up
+// to 0xFFFF; larger ones are gathered).
 SKY_DEV uint32_t scan_count(const DevBuffers& b, uint32_t i) {
-  return b.counts[b.perm ? b.perm[i] : i];
+  if (!b.perm) return b.counts[i];
+  const uint32_t c = b.ikeys_sorted[i] >> 16;
+  return c < 0xFFFFu ? c : b.counts[b.perm[i]];
 }
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevBuffers b, uint32_t n_items) {
@@ -226,14 +229,13 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const uint32_t v = blockIdx.y;
   if (g >= sp.n || v >= sp.num_views) return;
   const uint32_t pos = v * sp.n + g;  // position in emission (perm) order
-  // items of one sort group's views interleave: the sorted item key carries
-  // the item's own view and its depth field
+  // items of one sort group's views interleave: the view is the item's own;
+  // the sorted item key carries its depth field
   uint32_t item, view, dq;
   if (b.perm) {
     item = b.perm[pos];
-    const uint32_t ik = b.ikeys_sorted[pos];
-    view = ik >> 16;
-    dq = ik & 0xFFFFu;
+    view = item / sp.n;
+    dq = b.ikeys_sorted[pos] & 0xFFFFu;
   } else {
     item = pos;
     view = v;

@@ -75,7 +75,8 @@ struct DevBuffers {
   float2* aux;        // depth, radius per item
   uint32_t* counts;   // tiles per item
   uint2* rects;       // packed tile rectangle per item
-  uint32_t* ikeys;    // per item (view << 16) | depth16; sorted on depth16 per group
+  uint32_t* ikeys;    // per item (min(count, 0xFFFF) << 16) | depth16; sorted on depth16
+                      // per group
   uint32_t* ikeys_sorted;  // the item keys in emission (perm) order
   uint32_t* perm;     // item at each emission position: by (group, depth16, item)
                       // (NULL: item order)
