@@ -81,21 +81,26 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
 // Preprocess: one thread per Gaussian; its parameters are read (and rounded
 // to f16) once and projected into every view of the step.
 // ---------------------------------------------------------------------------
-// Three CTAs per multiprocessor (<= 85 registers): measured faster than two
-// with the parameters held unspilled.
-__global__ void __launch_bounds__(256, 3) k_preprocess(DevBuffers b) {
+// The SH coefficients live in shared memory (one column per thread,
+// conflict-free), the 11 geometry parameters in registers: 8 CTAs of 128
+// threads per multiprocessor.
+constexpr int kPrepThreads = 128;
+__global__ void __launch_bounds__(kPrepThreads, 8) k_preprocess(DevBuffers b) {
+  __shared__ float s_sh[48][kPrepThreads];
   const StepParams& sp = *b.sp;
-  const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = threadIdx.x;
+  const uint32_t g = blockIdx.x * blockDim.x + t;
   if (g >= sp.n) return;
   const bool r16 = sp.round_f16 != 0;
   const uint32_t stride = sp.plane_stride;
   const int deg = (int)sp.sh_deg;
   const int nsh = 3 * (deg + 1) * (deg + 1);
-  float prm[kPlanes];
+  float prm[11];
 #pragma unroll
-  for (int k = 0; k < kPlanes; ++k)
-    prm[k] = (k < 11 + nsh) ? load_plane(b.params, stride, k, g, r16) : 0.0f;
-  auto get = [&](int plane) { return prm[plane]; };
+  for (int k = 0; k < 11; ++k) prm[k] = load_plane(b.params, stride, k, g, r16);
+  for (int k = 0; k < 48; ++k)
+    s_sh[k][t] = k < nsh ? load_plane(b.params, stride, 11 + k, g, r16) : 0.0f;
+  auto get = [&](int plane) { return plane < 11 ? prm[plane] : s_sh[plane - 11][t]; };
   // the covariance, opacity and skip bound do not depend on the view
   GaussCov3 gc;
   gauss_cov3(get, gc);
@@ -1577,7 +1582,7 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
 // ---------------------------------------------------------------------------
 void launch_preprocess(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s) {
   (void)views;
-  k_preprocess<<<(n + 255) / 256, 256, 0, s>>>(b);
+  k_preprocess<<<(n + kPrepThreads - 1) / kPrepThreads, kPrepThreads, 0, s>>>(b);
 }
 
 void launch_scan(const DevBuffers& b, uint32_t n_items, cudaStream_t s) {
