@@ -61,7 +61,12 @@ def parse():
                          "mixed: 16 views per step of 640x480 / 1280x720 / 1920x1080; "
                          "stress4k: 4M tightly clustered SH-3 Gaussians, one 3840x2160 view")
     ap.add_argument("--tile-size", type=int, default=16, choices=[8, 16, 32])
-    ap.add_argument("--autotune", action="store_true", help="pick the tile size from 8/16/32 first")
+    ap.add_argument("--fwd-batch", type=int, default=0, choices=[0, 64, 128, 256],
+                    help="forward splat-batch depth (0 = 256)")
+    ap.add_argument("--bwd-batch", type=int, default=0, choices=[0, 32, 64, 128],
+                    help="16x16-tile backward splat-batch depth (0 = 128)")
+    ap.add_argument("--autotune", action="store_true",
+                    help="pick the tile size from 8/16/32, then the splat-batch depths")
     args = ap.parse_args()
     if args.workload == "stress4k":
         if args.n == 1_000_000:
@@ -317,9 +322,10 @@ def main():
 
     tune = None
     if args.autotune:
-        from skyfall.autotune import pick_tile_size
-        args.tile_size, tune = pick_tile_size(make, batched_sets[:3])
+        from skyfall.autotune import autotune
+        args.tile_size, args.fwd_batch, args.bwd_batch, tune = autotune(make, batched_sets[:3])
     r = make(args.tile_size)
+    r.setBatchDepth(args.fwd_batch, args.bwd_batch)
 
     def barrier():
         if world > 1:
@@ -404,7 +410,9 @@ def main():
         "config": {
             "workload": workload_name(args, n, B, C),
             "views_per_step": B, "global_batch": B, "parallelism": "replicas" if world > 1 else "none",
-            "tile_size": args.tile_size, "autotune_ms_per_step": tune,
+            "tile_size": args.tile_size, "fwd_batch": args.fwd_batch or 256,
+            "bwd_batch": (args.bwd_batch or 128) if args.tile_size == 16 else None,
+            "autotune_ms_per_step": tune,
             "l2": "inputs > L2 (no flush)",
         },
         "device_bytes": device_bytes,

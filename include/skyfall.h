@@ -104,6 +104,11 @@ typedef struct SkyConfig {
   uint32_t use_graph;          /* capture sky_step as one CUDA graph         */
   uint32_t max_views_per_step; /* batch size bound (buffers sized for it)    */
   uint64_t seed;               /* camera choice and densify randomness       */
+  uint32_t fwd_batch;          /* splat-batch depth of the forward: 64, 128,
+                                  256 (0 = 256)                              */
+  uint32_t bwd_batch;          /* of the 16x16-tile exact backward: 32, 64,
+                                  128 (0 = 128); neither changes a result,
+                                  both may change with sky_set_config        */
 } SkyConfig;
 
 typedef struct SkyStepStats {

@@ -114,6 +114,7 @@ struct Shape {
   uint32_t nv = 0, n = 0, stride = 0, mode = 0, icap = 0;
   uint32_t max_tiles = 0, max_view_px = 0, ngroups = 0;
   uint32_t key_bits[kMaxGroups] = {};
+  uint32_t fwd_batch = 0, bwd_batch = 0;  // splat-batch depths (kernel variants)
   bool with_loss = false, ssim = false, ref = false, prof = false;
   bool same(const Shape& o) const { return memcmp(this, &o, sizeof(Shape)) == 0; }
 };
@@ -366,13 +367,13 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
   TRY(mark(4));
   launch_ranges(b, c->icap, s);
   TRY(mark(5));
-  launch_forward(b, sh.max_tiles, c->cfg.tile_size, sh.ssim, sh.nv, sh.max_view_px, s);
+  launch_forward(b, sh.max_tiles, c->cfg.tile_size, sh.fwd_batch, sh.ssim, sh.nv, sh.max_view_px, s);
   if (sh.with_loss) launch_loss_final(b, s);
   launches += 4 + (sh.with_loss ? 1 : 0) + (sh.ssim ? 1 : 0);
   TRY(mark(6));
   if (sh.mode >= kBackward) {
     if (sh.ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
-    launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.ref, s);
+    launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.bwd_batch, sh.ref, s);
     TRY(mark(7));
     if (!sh.ref) {
       launch_item_sums(b, items, s);
@@ -553,6 +554,8 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   sh.ssim = with_loss && cfg.w_ssim > 0.0f;
   sh.ref = ref;
   sh.prof = c->profiling;
+  sh.fwd_batch = cfg.fwd_batch;
+  sh.bwd_batch = cfg.bwd_batch;
   cudaStream_t s = c->stream;
   uint64_t launches = 0;
   for (int attempt = 0;; ++attempt) {
@@ -1048,6 +1051,10 @@ static int check_cfg(const SkyConfig* cfg) {
     return fail(SKY_ERR_ARG, "tile_size %u not in {8, 16, 32}", cfg->tile_size);
   if (cfg->sh_degree > 3) return fail(SKY_ERR_ARG, "sh_degree %u > 3", cfg->sh_degree);
   if (cfg->backward_mode > 1) return fail(SKY_ERR_ARG, "unknown backward_mode");
+  if (cfg->fwd_batch != 0 && cfg->fwd_batch != 64 && cfg->fwd_batch != 128 && cfg->fwd_batch != 256)
+    return fail(SKY_ERR_ARG, "fwd_batch %u not in {0, 64, 128, 256}", cfg->fwd_batch);
+  if (cfg->bwd_batch != 0 && cfg->bwd_batch != 32 && cfg->bwd_batch != 64 && cfg->bwd_batch != 128)
+    return fail(SKY_ERR_ARG, "bwd_batch %u not in {0, 32, 64, 128}", cfg->bwd_batch);
   return SKY_OK;
 }
 

@@ -317,11 +317,12 @@ __global__ void k_ranges_empty(DevBuffers b) {
 // ---------------------------------------------------------------------------
 // Forward: training_tiled_forward (training-forward-tiles.wgsl:107-215), one
 // CTA per tile, one thread per pixel, splat records staged in shared memory
-// one batch of TS*TS at a time, whole-CTA early exit once every pixel has
-// reached the transmittance threshold.  The loss of training-loss.wgsl:86-126
-// (without its SSIM term) is fused into the epilogue.
+// one batch of FB (the splat-batch depth: 64, 128 or 256) at a time,
+// whole-CTA early exit once every pixel has reached the transmittance
+// threshold.  The loss of training-loss.wgsl:86-126 (without its SSIM term)
+// is fused into the epilogue.  The batch depth changes no result.
 // ---------------------------------------------------------------------------
-constexpr int kFwdBatch = 256;
+constexpr int kFwdBatch = 256;  // default splat-batch depth of the forward
 
 // Bit w set when warp w of the tile (pixel rows [w * RPW, (w + 1) * RPW),
 // RPW = 32/TS unless the warp's lanes hold several pixels) has a pixel centre
@@ -367,13 +368,14 @@ SKY_DEV uint32_t warp_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
   return upto & ~((1u << wlo) - 1u);
 }
 
-template <int TS>
+template <int TS, int FB>
 __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
+  static_assert(FB <= 256, "list entries are bytes");
   constexpr int NT = TS * TS;
   constexpr int NW = NT / 32;
-  __shared__ float4 s_rec[kFwdBatch * 3];
-  __shared__ uint32_t s_mask[kFwdBatch];
-  __shared__ uint8_t s_list[NW][kFwdBatch];
+  __shared__ float4 s_rec[FB * 3];
+  __shared__ uint32_t s_mask[FB];
+  __shared__ uint8_t s_list[NW][FB];
   __shared__ double s_loss[NW];
   const StepParams& sp = *b.sp;
   const uint32_t tile = blockIdx.x;
@@ -398,8 +400,8 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   bool done = !inside;
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
-  for (uint32_t bs = start; bs < end; bs += kFwdBatch) {
-    const uint32_t cnt = min((uint32_t)kFwdBatch, end - bs);
+  for (uint32_t bs = start; bs < end; bs += FB) {
+    const uint32_t cnt = min((uint32_t)FB, end - bs);
     __syncthreads();
     for (uint32_t k = tid; k < cnt; k += NT) {
       const size_t r = b.flatten[bs + k];
@@ -868,8 +870,12 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
   return true;
 }
 
+// BB: the splat-batch depth (32, 64 or 128 staged splats); the per-splat sums
+// do not depend on it.
+template <int BB>
 __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
-  constexpr int TS = 16, NT = 128, NW = 4, kBatch = 128;
+  static_assert(BB <= 256, "list entries are bytes");
+  constexpr int TS = 16, NT = 128, NW = 4, kBatch = BB;
   __shared__ float4 s_rec[kBatch * 3];
   __shared__ uint32_t s_mask[kBatch];
   __shared__ float s_part[NW][kBatch][9];
@@ -1610,13 +1616,22 @@ void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s) {
   k_ranges_empty<<<1, 256, 0, s>>>(b);
 }
 
-void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ssim,
+template <int TS>
+void launch_forward_ts(const DevBuffers& b, uint32_t max_tiles, uint32_t fb, cudaStream_t s) {
+  switch (fb) {
+    case 64: k_forward<TS, 64><<<max_tiles, TS * TS, 0, s>>>(b); break;
+    case 128: k_forward<TS, 128><<<max_tiles, TS * TS, 0, s>>>(b); break;
+    default: k_forward<TS, kFwdBatch><<<max_tiles, TS * TS, 0, s>>>(b); break;
+  }
+}
+
+void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t fb, bool ssim,
                     uint32_t views, uint32_t max_view_pixels, cudaStream_t s) {
   if (max_tiles == 0) return;
   switch (ts) {
-    case 8: k_forward<8><<<max_tiles, 64, 0, s>>>(b); break;
-    case 32: k_forward<32><<<max_tiles, 1024, 0, s>>>(b); break;
-    default: k_forward<16><<<max_tiles, 256, 0, s>>>(b); break;
+    case 8: launch_forward_ts<8>(b, max_tiles, fb, s); break;
+    case 32: launch_forward_ts<32>(b, max_tiles, fb, s); break;
+    default: launch_forward_ts<16>(b, max_tiles, fb, s); break;
   }
   if (ssim) {
     dim3 grid((max_view_pixels + 255) / 256, views);
@@ -1626,13 +1641,20 @@ void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool s
 
 void launch_loss_final(const DevBuffers& b, cudaStream_t s) { k_loss_final<<<1, 1024, 0, s>>>(b); }
 
-void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, bool ref, cudaStream_t s) {
+void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t bb, bool ref,
+                     cudaStream_t s) {
   if (max_tiles == 0) return;
   if (!ref) {
     switch (ts) {
       case 8: k_backward_exact<8><<<max_tiles, 64, 0, s>>>(b); break;
       case 32: k_backward_exact<32><<<max_tiles, 1024, 0, s>>>(b); break;
-      default: k_backward_exact2<<<max_tiles, 128, 0, s>>>(b); break;
+      default:
+        switch (bb) {
+          case 32: k_backward_exact2<32><<<max_tiles, 128, 0, s>>>(b); break;
+          case 64: k_backward_exact2<64><<<max_tiles, 128, 0, s>>>(b); break;
+          default: k_backward_exact2<kBwdBatch16><<<max_tiles, 128, 0, s>>>(b); break;
+        }
+        break;
     }
   } else {
     switch (ts) {

@@ -316,6 +316,13 @@ class GaussianRenderer:
             setattr(self.config, k, v)
         L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
 
+    def setBatchDepth(self, fwd_batch: int = 0, bwd_batch: int = 0) -> None:
+        """Splat-batch depths of the rasterizers (0 = default); results do not
+        depend on them, only speed (see skyfall.autotune)."""
+        self.config.fwd_batch = fwd_batch
+        self.config.bwd_batch = bwd_batch
+        L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
+
     def getLossWeights(self) -> LossWeights:
         return LossWeights(self.config.w_l2, self.config.w_l1, self.config.w_ssim)
 

@@ -48,6 +48,12 @@ def test_config_size_is_checked_before_touching_the_device(sky):
     assert b"SkyConfig size" in L.sky_last_error()
     c = sky.default_config(tile_size=12)
     assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
+    # splat-batch depths outside the compiled variants are refused up front
+    for kw in (dict(fwd_batch=100), dict(fwd_batch=512), dict(bwd_batch=256), dict(bwd_batch=16)):
+        c = sky.default_config(**kw)
+        assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
+        assert b"batch" in L.sky_last_error()
+    assert sky.default_config().fwd_batch == 0 and sky.default_config().bwd_batch == 0
 
 
 def test_pinhole_camera_matches_reference_projection(sky):

@@ -165,3 +165,46 @@ def test_tile_size_autotuner(sky):
     best, times = pick_tile_size(make, [[0, 1, 2, 3]] * 3)
     assert best in (8, 16, 32) and set(times) == {8, 16, 32}
     assert all(t > 0 for t in times.values()) and times[best] == min(times.values())
+    from skyfall.autotune import autotune
+    ts, fb, bb, tt = autotune(make, [[0, 1, 2, 3]] * 3)
+    assert ts in (8, 16, 32) and fb in (64, 128, 256)
+    assert set(tt["fwd_batch"]) == {64, 128, 256} and tt["fwd_batch"][fb] == min(tt["fwd_batch"].values())
+    if ts == 16:
+        assert bb in (32, 64, 128) and tt["bwd_batch"][bb] == min(tt["bwd_batch"].values())
+    else:
+        assert bb == 0 and tt["bwd_batch"] == {}
+
+
+def test_splat_batch_depths_change_no_result(sky):
+    """Every forward depth gives the same images, alphas, last indices and
+    loss, every backward depth the same gradients, bit for bit (the batch
+    only sets how many splats are staged at once)."""
+    from skyfall import scenes
+    P = scenes.scene_clusters(20000, seed=1601, clusters=16, center_range=1.0, cluster_sigma=0.25,
+                              logscale_mean=-3.8)
+    cams = scenes.cameras_orbit(2, 3.5, 240, 176)
+    tgts = [scenes.target_uniform(240, 176, seed=2600 + k) for k in range(2)]
+    r = make(sky, P, cams, tgts, sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2,
+             w_ssim=0.0, tile_size=16)
+    ref = None
+    for fb, bb in [(0, 0), (64, 32), (128, 64), (256, 128), (64, 128)]:
+        r.setBatchDepth(fb, bb)
+        loss = r.forward([0, 1])
+        out = (loss, r.read_buffer("color"), r.read_buffer("alpha"), r.read_buffer("last_ids"),
+               r.backward())
+        if ref is None:
+            ref = out
+            continue
+        assert out[0] == ref[0]
+        for a, b in zip(out[1:], ref[1:]):
+            assert np.array_equal(a, b)
+    # and on the graph-captured training path, a changed depth re-captures
+    r.close()
+    r = make(sky, P, cams, tgts, sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2,
+             w_ssim=0.0, tile_size=16, use_graph=1)
+    for fb, bb in [(0, 0), (0, 0), (64, 32), (64, 32)]:
+        r.setBatchDepth(fb, bb)
+        r.trainStep([0, 1])
+    st = r.getStatus()
+    # step 1 runs directly, step 2 captures, step 3 re-captures, step 4 replays
+    assert st.graph_captures == 2 and st.graph_replays == 3
