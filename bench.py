@@ -67,6 +67,8 @@ def parse():
                     help="16x16-tile backward splat-batch depth (0 = 128)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the tile size from 8/16/32, then the splat-batch depths")
+    ap.add_argument("--prune-after", action="store_true",
+                    help="after the measurement, prune a seeded 10%% of the Gaussians once")
     args = ap.parse_args()
     if args.workload == "stress4k":
         if args.n == 1_000_000:
@@ -434,6 +436,15 @@ def main():
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
+    if args.prune_after:
+        # After the timed region: one prune of a seeded 10 % of the Gaussians
+        # through the public API (the compaction kernels an ncu capture of
+        # this command measures); the wall time includes the host work.
+        mask = np.random.default_rng(7).random(r.getGaussianCount()) < 0.1
+        t0 = time.perf_counter()
+        left = r.prune(minOpacity=0.0, mask=mask.astype(np.uint8))
+        line["prune"] = {"removed": int(mask.sum()), "remaining": int(left),
+                         "wall_ms": (time.perf_counter() - t0) * 1e3}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

@@ -32,16 +32,22 @@ __global__ void k_prune_flags(const float* __restrict__ P, uint32_t stride, uint
 }
 
 // dst plane k, position scan[i] - 1 <- src plane k, position i, for survivors.
-__global__ void k_compact(const float* __restrict__ src, float* __restrict__ dst,
-                          uint32_t src_stride, uint32_t dst_stride, uint32_t planes, uint32_t n,
-                          const uint32_t* __restrict__ keep_scan) {
+// One thread per Gaussian walks all planes (the survivor test is read once;
+// eight plane loads in flight per thread), neighbouring threads touching
+// neighbouring addresses of each plane.
+__global__ void __launch_bounds__(256) k_compact(const float* __restrict__ src, float* __restrict__ dst,
+                                                 uint32_t src_stride, uint32_t dst_stride,
+                                                 uint32_t planes, uint32_t n,
+                                                 const uint32_t* __restrict__ keep_scan) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  const uint32_t k = blockIdx.y;
-  if (i >= n || k >= planes) return;
+  if (i >= n) return;
   const uint32_t incl = keep_scan[i];
   const uint32_t prev = i ? keep_scan[i - 1] : 0u;
   if (incl == prev) return;
-  dst[(size_t)k * dst_stride + (incl - 1)] = src[(size_t)k * src_stride + i];
+  const size_t d = incl - 1;
+#pragma unroll 8
+  for (uint32_t k = 0; k < planes; ++k)
+    dst[(size_t)k * dst_stride + d] = src[(size_t)k * src_stride + i];
 }
 
 __global__ void k_reset_opacity(float* __restrict__ P, uint32_t stride, uint32_t n, float max_logit) {
@@ -63,8 +69,7 @@ void launch_prune_flags(const float* params, uint32_t stride, uint32_t n, float 
 void launch_compact(const float* src, float* dst, uint32_t src_stride, uint32_t dst_stride,
                     uint32_t planes, uint32_t n, const uint32_t* keep_scan, cudaStream_t s) {
   if (n == 0) return;
-  dim3 grid((n + 255) / 256, planes);
-  k_compact<<<grid, 256, 0, s>>>(src, dst, src_stride, dst_stride, planes, n, keep_scan);
+  k_compact<<<(n + 255) / 256, 256, 0, s>>>(src, dst, src_stride, dst_stride, planes, n, keep_scan);
 }
 
 void launch_reset_opacity(float* params, uint32_t stride, uint32_t n, float max_logit,
