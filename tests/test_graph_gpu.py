@@ -36,6 +36,30 @@ def test_graph_replay_matches_direct_launches(sky):
     assert np.array_equal(out[0][2][0], out[1][2][0]) and np.array_equal(out[0][2][1], out[1][2][1])
 
 
+def test_graph_replay_matches_direct_with_two_sort_groups(sky):
+    """1920x1080 views at 8-pixel tiles (32,400 tiles each): a step of three
+    views splits into two sort groups, each with its own depth-ordered item
+    pass; graph replays and direct launches must still agree bit for bit."""
+    P = scenes.scene_clusters(20000, seed=54, clusters=8, center_range=1.0, logscale_mean=-4.0)
+    cams = scenes.cameras_orbit(3, 3.5, 1920, 1080)
+    tgt = [scenes.target_uniform(1920, 1080, seed=80 + k) for k in range(3)]
+    plan = [[0, 1, 2], [2, 1, 0], [1, 2, 0]]
+    out = []
+    for graph in (False, True):
+        r = sky.GaussianRenderer(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0,
+                                 use_graph=int(graph), sh_update_interval=2, tile_size=8)
+        r.load_points(P)
+        r.setTrainingCameras(cams)
+        r.setTrainingImages(tgt)
+        losses = [r.trainStep(v).loss for v in plan]
+        assert r.read_buffer("groups").reshape(-1, 2).shape[0] == 2
+        out.append((losses, r.params(), r.moments()))
+        r.close()
+    assert out[0][0] == out[1][0]
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][2][0], out[1][2][0]) and np.array_equal(out[0][2][1], out[1][2][1])
+
+
 def test_graph_regrows_capacity(sky):
     P = scenes.scene_clusters(40000, seed=53, clusters=8, center_range=1.0, logscale_mean=-4.0)
     far = scenes.camera_fov((0.0, 0.5, 14.0), 160, 120)
