@@ -175,6 +175,39 @@ def test_tile_size_autotuner(sky):
         assert bb == 0 and tt["bwd_batch"] == {}
 
 
+def test_views_with_nothing_in_front(sky, orc):
+    """A view that sees no Gaussian: its items have no tiles, its sort-group
+    segment or its share of one is empty.  Batched with a normal view it
+    renders the background and adds nothing to the gradients; a step of empty
+    views only gives zero gradients; the graph path runs such steps too."""
+    P = scenes.scene_uniform(8192, seed=37)
+    normal = scenes.cameras_single(64, 64, 3.0)[0]
+    away = scenes.camera_fov((0.0, 0.0, -3.0), 64, 64, target=(0.0, 0.0, -10.0))
+    cams = [away, normal]
+    tgt = [scenes.target_uniform(64, 64, seed=38), scenes.target_uniform(64, 64, seed=39)]
+    cfg = dict(sh_degree=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0)
+    r = make(sky, P, cams, tgt, **cfg)
+    r.forward([1])
+    g_normal = r.backward()
+    loss = r.forward([0, 1])
+    g_both = r.backward()
+    assert np.array_equal(g_both, g_normal)
+    rgba = r.read_buffer("color").reshape(-1, 4)
+    assert not rgba[:64 * 64, :3].any() and not r.read_buffer("alpha")[:64 * 64].any()
+    s = orc.settings(w_l2=1.0, w_l1=0.2, w_ssim=0.0)
+    ref = orc.view_pipeline(P, normal, tgt[1], s, 0, mode=0)
+    assert np.array_equal(rgba[64 * 64:], ref["fw"]["rgba"])
+    r.forward([0, 0])
+    assert not r.backward().any()
+    assert r.read_buffer("counts").sum() == 0
+    r.close()
+    r = make(sky, P, cams, tgt, use_graph=1, **cfg)
+    for views in ([0, 1], [0, 1], [0, 0], [1, 0]):
+        st = r.trainStep(views)
+        assert np.isfinite(st.loss)
+    assert np.all(np.isfinite(r.params()))
+
+
 def test_splat_batch_depths_change_no_result(sky):
     """Every forward depth gives the same images, alphas, last indices and
     loss, every backward depth the same gradients, bit for bit (the batch
