@@ -259,6 +259,7 @@ void sky_config_default(SkyConfig* cfg);
 int sky_create(const SkyConfig* cfg, void** ctx_out);
 int sky_destroy(void* ctx);
 int sky_set_config(void* ctx, const SkyConfig* cfg); /* mutable fields only   */
+int sky_get_config(void* ctx, SkyConfig* out);       /* the context's config  */
 const char* sky_last_error(void);
 int sky_version(void);
 

@@ -1121,6 +1121,13 @@ int sky_set_config(void* p, const SkyConfig* cfg) {
   return SKY_OK;
 }
 
+int sky_get_config(void* p, SkyConfig* out) {
+  Context* c = as_ctx(p);
+  if (!c || !out) return fail(SKY_ERR_ARG, "bad arguments");
+  *out = c->cfg;
+  return SKY_OK;
+}
+
 int sky_camera_pinhole(const float view[16], double fx, double fy, double cx, double cy,
                        uint32_t width, uint32_t height, SkyCamera* out) {
   if (!view || !out || width == 0 || height == 0) return fail(SKY_ERR_ARG, "bad camera");

@@ -145,6 +145,7 @@ PROTOTYPES = {
     "sky_create": (I32, [C.POINTER(SkyConfig), C.POINTER(C.c_void_p)]),
     "sky_destroy": (I32, [P]),
     "sky_set_config": (I32, [P, C.POINTER(SkyConfig)]),
+    "sky_get_config": (I32, [P, C.POINTER(SkyConfig)]),
     "sky_camera_pinhole": (I32, [P, C.c_double, C.c_double, C.c_double, C.c_double, U32, U32,
                                  C.POINTER(SkyCamera)]),
     "sky_load_points": (I32, [P, P, U32, U64]),

@@ -316,6 +316,13 @@ class GaussianRenderer:
             setattr(self.config, k, v)
         L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
 
+    def getConfig(self) -> L.SkyConfig:
+        """The context's configuration as the library holds it."""
+        c = L.SkyConfig()
+        c.struct_size = C.sizeof(L.SkyConfig)
+        L.check(self._L.sky_get_config(self._h, C.byref(c)))
+        return c
+
     def setBatchDepth(self, fwd_batch: int = 0, bwd_batch: int = 0) -> None:
         """Splat-batch depths of the rasterizers (0 = default); results do not
         depend on them, only speed (see skyfall.autotune)."""

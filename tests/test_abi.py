@@ -77,4 +77,6 @@ def test_null_context_and_argument_errors(sky):
     assert L.sky_render(None, None, 0, None, None) == E.SKY_ERR_ARG
     assert L.sky_destroy(None) == 0
     assert L.sky_sort_pairs(None, None, None, None, 4, 8, None) == E.SKY_ERR_ARG
+    c = sky.default_config()
+    assert L.sky_get_config(None, C.byref(c)) == E.SKY_ERR_ARG
     assert L.sky_version() == 1

@@ -222,6 +222,8 @@ def test_splat_batch_depths_change_no_result(sky):
     ref = None
     for fb, bb in [(0, 0), (64, 32), (128, 64), (256, 128), (64, 128)]:
         r.setBatchDepth(fb, bb)
+        got = r.getConfig()
+        assert (got.fwd_batch, got.bwd_batch, got.tile_size) == (fb, bb, 16)
         loss = r.forward([0, 1])
         out = (loss, r.read_buffer("color"), r.read_buffer("alpha"), r.read_buffer("last_ids"),
                r.backward())
