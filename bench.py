@@ -372,8 +372,8 @@ def main():
     # intersection: the 48-byte record, its 4-byte item index and the 48-byte
     # partial; per pixel: last index, transmittance, residual.
     algo_bytes = {
-        "preprocess": n * 236 + B * n * 64,
-        "scan": B * n * 8,
+        "preprocess": n * 236 + B * n * 72,
+        "scan": B * n * 16,
         "emit": isect * 8 + B * n * 20,
         "sort": isect * 36,
         "ranges": isect * 4,
