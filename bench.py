@@ -118,6 +118,17 @@ def measured_traffic(kernel: str, workload: str):
     return float(e["bytes_per_launch"])
 
 
+def measured_issue(kernel: str):
+    """Issue-slot utilisation of `kernel` (smsp__issue_active, fraction of
+    cycles a warp instruction issued) from its full ncu capture, recorded in
+    profiles/traffic.json: the bound of the issue-bound raster kernels."""
+    p = REPO / "profiles" / "traffic.json"
+    if not p.exists():
+        return None
+    e = json.loads(p.read_text()).get(kernel) or {}
+    return e.get("issue_active")
+
+
 def render_targets(sky, cams, args):
     """Targets: renders of a separate ground-truth scene."""
     from skyfall import scenes
@@ -432,7 +443,13 @@ def main():
                      "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "algorithmic_bytes": algo_bytes[dom],
                      "traffic_source": "profiles/traffic.json (ncu dram__bytes_read.sum + "
-                                       "dram__bytes_write.sum, same workload)" if traffic else None},
+                                       "dram__bytes_write.sum, same workload)" if traffic else None,
+                     # the raster kernels are issue-bound: the fraction of cycles on
+                     # which a warp instruction issued (full ncu capture of the kernel)
+                     "issue_active": measured_issue(dom),
+                     "issue_source": "profiles/traffic.json (ncu smsp__issue_active, "
+                                     "profiles/raster_and_sort_4views_200k_1080p.md)"
+                                     if measured_issue(dom) is not None else None},
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
