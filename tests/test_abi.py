@@ -80,3 +80,46 @@ def test_null_context_and_argument_errors(sky):
     c = sky.default_config()
     assert L.sky_get_config(None, C.byref(c)) == E.SKY_ERR_ARG
     assert L.sky_version() == 1
+
+
+C_PROGRAM = r"""
+#include <stdio.h>
+#include <string.h>
+#include "skyfall.h"
+
+int main(void) {
+  SkyConfig cfg;
+  sky_config_default(&cfg);
+  if (cfg.struct_size != sizeof(SkyConfig) || cfg.tile_size != 16) return 1;
+  void* ctx = NULL;
+  cfg.tile_size = 12;                       /* refused before any device call */
+  if (sky_create(&cfg, &ctx) != SKY_ERR_ARG || ctx != NULL) return 2;
+  if (strstr(sky_last_error(), "tile_size") == NULL) return 3;
+  if (sky_get_count(NULL, NULL) != SKY_ERR_ARG) return 4;
+  SkyCamera cam;
+  float view[16] = {1,0,0,0, 0,1,0,0, 0,0,1,0, 0,0,3,1};
+  if (sky_camera_pinhole(view, 100.0, 100.0, 32.0, 24.0, 64, 48, &cam) != SKY_OK) return 5;
+  printf("%d %u %u %.3f\n", sky_version(), cam.width, cam.height, cam.proj[0]);
+  return 0;
+}
+"""
+
+
+def test_header_is_c99_and_links_from_c(sky, tmp_path):
+    """include/skyfall.h compiles as C99 and a C program links and calls the
+    library -- what a cgo / N-API / FFI binding does (no device calls)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "abi.c"
+    src.write_text(C_PROGRAM)
+    libdir = sky._lib.LIB_PATH.parent
+    exe = tmp_path / "abi"
+    subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-pedantic", f"-I{REPO / 'include'}", str(src),
+                    f"-L{libdir}", "-lskyfall", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, (out.returncode, out.stderr)
+    ver, w, h, sx = out.stdout.split()
+    assert (int(ver), int(w), int(h)) == (1, 64, 48) and float(sx) == pytest.approx(2 * 100 / 64, rel=1e-6)
