@@ -5,6 +5,8 @@
 #include "kernels.cuh"
 #include "project.cuh"
 
+#include <atomic>
+
 namespace sky {
 namespace {
 
@@ -1667,12 +1669,14 @@ void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint3
 
 void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s) {
   if (n == 0) return;
-  static bool smem_set[64] = {};  // per device: the opt-in above 48 KB
+  // per device: the opt-in above 48 KB of shared memory (idempotent, so two
+  // threads that both see it unset both set it)
+  static std::atomic<bool> smem_set[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
-  if (!smem_set[dev]) {
+  if (!smem_set[dev].load(std::memory_order_acquire)) {
     cudaFuncSetAttribute(k_geom_adam, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kGeomSmem);
-    smem_set[dev] = true;
+    smem_set[dev].store(true, std::memory_order_release);
   }
   k_geom_adam<<<(n + kGeomThreads - 1) / kGeomThreads, kGeomThreads, kGeomSmem, s>>>(b);
 }

@@ -1,6 +1,9 @@
 // Onesweep LSD radix sort (see sort.cuh).
 #include "sort.cuh"
 
+#include <algorithm>
+#include <atomic>
+
 namespace sky {
 namespace {
 
@@ -316,15 +319,16 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
 }  // namespace
 
 int sm_count() {
-  static int cache[64] = {};
+  static std::atomic<int> cache[64];  // per device; threads racing to fill it store the same value
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) dev = 0;
-  if (!cache[dev]) {
-    int v = 0;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (!v) {
     cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    cache[dev] = v > 0 ? v : 132;
+    if (v <= 0) v = 132;
+    cache[dev].store(v, std::memory_order_relaxed);
   }
-  return cache[dev];
+  return v;
 }
 
 size_t sort_scratch_bytes(uint32_t max_n) {
