@@ -353,6 +353,46 @@ SKY_DEV uint32_t block_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
   return mask;
 }
 
+// block_mask with the bounding box replaced, block by block, by the ellipse
+// itself: bit w is cleared when s = 0.5 (a dx^2 + c dy^2) + b dx dy exceeds
+// smax at every pixel centre of block w, so no pixel there can pass the
+// raster pre-filter and the block's warp would do nothing with the splat.
+// Per block, dx runs over [u0, u1] = the f32 values px - mx of the block's
+// first and last columns (the kernels' own dx, monotone in px), dy likewise;
+// the minimum of the convex s over that rectangle lies on one of its edges
+// (or is 0 when the rectangle holds the mean): along an edge u = u0 it is at
+// v = -b u0 / c clamped to [v0, v1].  Rounding: for a conic with
+// b^2 <= 0.98 a c, |a dx^2| + |c dy^2| + 2 |b dx dy| <= 400 s, so an f32
+// evaluation of s (the kernels' and this one) is within 3e-4 s of the exact
+// value; a block is dropped only when the computed minimum exceeds
+// 1.001 smax.  Worse-conditioned conics keep the bounding-box mask.
+template <int TS, int BW, int BH>
+SKY_DEV uint32_t ellipse_mask(float4 r0, float4 r1, float4 r2, uint32_t x0, uint32_t y0) {
+  constexpr int NCOL = TS / BW;
+  uint32_t m = block_mask<TS, BW, BH>(r0, r2, x0, y0);
+  const float a = r0.z, bq = r0.w, c = r1.x;
+  if (m == 0u || !(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c))) return m;
+  const float lim = 1.001f * r2.y;
+  // edge minimisers per unit offset; an error in them only moves the point
+  // along the edge, raising s there by a relative O(ulp^2)
+  const float ku = -__fdividef(bq, c), kv = -__fdividef(bq, a);
+  auto s_at = [&](float u, float v) { return 0.5f * ((a * u) * u + (c * v) * v) + (bq * u) * v; };
+  for (uint32_t rest = m; rest != 0u; rest &= rest - 1u) {
+    const int w = __ffs(rest) - 1;
+    const float cx = (float)(x0 + (uint32_t)((w % NCOL) * BW)) + 0.5f;
+    const float cy = (float)(y0 + (uint32_t)((w / NCOL) * BH)) + 0.5f;
+    const float u0 = cx - r0.x, u1 = (cx + (float)(BW - 1)) - r0.x;
+    const float v0 = cy - r0.y, v1 = (cy + (float)(BH - 1)) - r0.y;
+    if (u0 <= 0.0f && u1 >= 0.0f && v0 <= 0.0f && v1 >= 0.0f) continue;
+    float smin = s_at(u0, fminf(fmaxf(ku * u0, v0), v1));
+    smin = fminf(smin, s_at(u1, fminf(fmaxf(ku * u1, v0), v1)));
+    smin = fminf(smin, s_at(fminf(fmaxf(kv * v0, u0), u1), v0));
+    smin = fminf(smin, s_at(fminf(fmaxf(kv * v1, u0), u1), v1));
+    if (smin > lim) m &= ~(1u << w);
+  }
+  return m;
+}
+
 template <int TS, int RPW = 32 / TS>
 SKY_DEV uint32_t warp_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
   const float hx = r2.z, hy = r2.w;
@@ -939,11 +979,12 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
     for (int k = (int)tid; k < cnt; k += NT) {
       const size_t r = b.flatten[bhi - k];
       const float4 q0 = b.records[r * 3 + 0];
+      const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
       s_rec[k * 3 + 0] = q0;
-      s_rec[k * 3 + 1] = b.records[r * 3 + 1];
+      s_rec[k * 3 + 1] = q1;
       s_rec[k * 3 + 2] = q2;
-      s_mask[k] = block_mask<TS, 8, 8>(q0, q2, tx * TS, ty * TS);
+      s_mask[k] = ellipse_mask<TS, 8, 8>(q0, q1, q2, tx * TS, ty * TS);
     }
     __syncthreads();
     uint32_t nlist = 0;
