@@ -410,6 +410,22 @@ SKY_DEV uint32_t warp_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
   return upto & ~((1u << wlo) - 1u);
 }
 
+// A raster record as the tiled kernels keep it in shared memory: the conic's
+// a and c halved, so that (a/2 dx) dx + (c/2 dy) dy is the reference's
+// 0.5 (a dx^2 + c dy^2) bit for bit (halving is exact, and for the emitted
+// conics, a, c >= 1e-6 and |dx|, |dy| = 0 or >= 2^-26, no product comes near
+// the subnormal range), one multiply fewer per pixel and splat.
+SKY_DEV void stage_record(float4* dst, const float4& q0, const float4& q1, const float4& q2) {
+  dst[0] = make_float4(q0.x, q0.y, 0.5f * q0.z, q0.w);
+  dst[1] = make_float4(0.5f * q1.x, q1.y, q1.z, q1.w);
+  dst[2] = q2;
+}
+
+// !(0 <= s <= smax) for smax > 0 (every listed splat's) in one unsigned
+// compare: a negative s has the sign bit set, and s is never -0 (it is
+// (+0 or positive) + (b dx) dy, and +0 + -0 = +0).
+SKY_DEV bool outside_smax(float s, float smax) { return __float_as_uint(s) > __float_as_uint(smax); }
+
 template <int TS, int FB>
 __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   static_assert(FB <= 256, "list entries are bytes");
@@ -448,10 +464,9 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
     for (uint32_t k = tid; k < cnt; k += NT) {
       const size_t r = b.flatten[bs + k];
       const float4 q0 = b.records[r * 3 + 0];
+      const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
-      s_rec[k * 3 + 0] = q0;
-      s_rec[k * 3 + 1] = b.records[r * 3 + 1];
-      s_rec[k * 3 + 2] = q2;
+      stage_record(s_rec + k * 3, q0, q1, q2);
       s_mask[k] = block_mask<TS, 8, 4>(q0, q2, tx * TS, ty * TS);
     }
     __syncthreads();
@@ -472,12 +487,12 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
         const float4 r0 = s_rec[j * 3 + 0];
         const float4 r2 = s_rec[j * 3 + 2];
         const float dx = pxf - r0.x, dy = pyf - r0.y;
-        const float s1 = (r0.z * dx) * dx;
+        const float s1 = (r0.z * dx) * dx;  // halved conic: s1 + s2 = 0.5 (a dx^2 + c dy^2)
         const float4 r1 = s_rec[j * 3 + 1];
         const float s2 = (r1.x * dy) * dy;
-        float so2 = 0.5f * (s1 + s2);
+        float so2 = s1 + s2;
         so2 = so2 + (r0.w * dx) * dy;
-        if (so2 < 0.0f || so2 > r2.y) continue;
+        if (outside_smax(so2, r2.y)) continue;
         // emitted records have finite means and conics, so 0 <= s <= s_max
         const float G = sky_expf_inrange(-so2);
         const float al = r1.y * G;
@@ -871,15 +886,16 @@ SKY_DEV float exp_neg_approx(float s) {
 // values only have to be accurate.  So alpha comes from the fast exponential,
 // and from sky_expf (the forward's) only when it lies within 2e-6 relative of
 // either threshold, where the two could decide differently.
-// dx = px - mx, s1 = (a dx) dx and bdx = b dx belong to the pixel column and
-// are shared by the lane's two pixels.
+// dx = px - mx, s1 = (a/2 dx) dx (q0, q1 are staged records, conic halved)
+// and bdx = b dx belong to the pixel column and are shared by the lane's two
+// pixels.
 SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0, const float4& q1,
                       const float4& q2, float val[9]) {
   const float dy = p.py - q0.y;
-  const float s2 = (q1.x * dy) * dy;
-  float so2 = 0.5f * (s1 + s2);
+  const float s2 = (q1.x * dy) * dy;  // staged record: halved conic
+  float so2 = s1 + s2;
   so2 = so2 + bdx * dy;
-  if (!(so2 >= 0.0f && so2 <= q2.y)) return false;
+  if (outside_smax(so2, q2.y)) return false;
   float G = exp_neg_approx(so2);
   float al = q1.y * G;
   if (fabsf(al - MIN_ALPHA) <= 2e-6f * MIN_ALPHA || fabsf(al - MAX_ALPHA) <= 2e-6f) {
@@ -981,9 +997,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float4 q0 = b.records[r * 3 + 0];
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
-      s_rec[k * 3 + 0] = q0;
-      s_rec[k * 3 + 1] = q1;
-      s_rec[k * 3 + 2] = q2;
+      stage_record(s_rec + k * 3, q0, q1, q2);
       s_mask[k] = ellipse_mask<TS, 8, 8>(q0, q1, q2, tx * TS, ty * TS);
     }
     __syncthreads();
@@ -1034,10 +1048,11 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
         for (int k = 0; k < 9; ++k) sum[k] = sum[k] + s_part[w][j][k];
       }
       const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1];
+      const float ca = q0.z + q0.z, cc = q1.x + q1.x;  // the conic (exact doubling)
       const float dlogit = sum[3] * (1.0f - q1.y);
       const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
-      const float dmx = __fmaf_rn(q0.z, sum[7], q0.w * sum[8]);
-      const float dmy = __fmaf_rn(q0.w, sum[7], q1.x * sum[8]);
+      const float dmx = __fmaf_rn(ca, sum[7], q0.w * sum[8]);
+      const float dmy = __fmaf_rn(q0.w, sum[7], cc * sum[8]);
       float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
       dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
       dst[1] = make_float4(dca, dcb, dcc, dmx);
