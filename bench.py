@@ -65,6 +65,9 @@ def parse():
                     help="forward splat-batch depth (0 = 256)")
     ap.add_argument("--bwd-batch", type=int, default=0, choices=[0, 32, 64, 128],
                     help="16x16-tile backward splat-batch depth (0 = 128)")
+    ap.add_argument("--tile-cull", type=int, default=1, choices=[0, 1],
+                    help="1: intersection lists of the training steps hold only the tiles each "
+                         "Gaussian's alpha >= 1/255 ellipse reaches (bit-identical results)")
     ap.add_argument("--autotune", action="store_true",
                     help="pick the tile size from 8/16/32, then the splat-batch depths")
     ap.add_argument("--prune-after", action="store_true",
@@ -331,6 +334,7 @@ def main():
         rr.load_points(P)
         rr.setTrainingCameras(cams)
         rr.setTrainingImages(targets)
+        rr.setTileCull(bool(args.tile_cull))
         return rr
 
     tune = None
@@ -395,7 +399,7 @@ def main():
     peak, peak_kind = measured_peak()
     achieved = algo_bytes[dom] / (stage_ms[dom] / 1000.0) / 1e9
     clocks = clk.summary()
-    wl_key = f"{args.workload}/ts{args.tile_size}"
+    wl_key = f"{args.workload}/ts{args.tile_size}" + ("/cull" if args.tile_cull else "")
     traffic = measured_traffic(dom, wl_key)
 
     cpu = None
@@ -425,6 +429,7 @@ def main():
             "views_per_step": B, "global_batch": B, "parallelism": "replicas" if world > 1 else "none",
             "tile_size": args.tile_size, "fwd_batch": args.fwd_batch or 256,
             "bwd_batch": (args.bwd_batch or 128) if args.tile_size == 16 else None,
+            "tile_cull": bool(args.tile_cull),
             "autotune_ms_per_step": tune,
             "l2": "inputs > L2 (no flush)",
         },

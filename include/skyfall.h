@@ -109,6 +109,18 @@ typedef struct SkyConfig {
   uint32_t bwd_batch;          /* of the 16x16-tile exact backward: 32, 64,
                                   128 (0 = 128); neither changes a result,
                                   both may change with sky_set_config        */
+  uint32_t tile_cull;          /* 1: the intersection lists of backward and
+                                  training steps in the exact backward mode
+                                  hold only the tiles of each Gaussian's
+                                  rectangle that its alpha >= 1/255 ellipse
+                                  reaches.  Images, loss, gradients,
+                                  statistics and parameters are
+                                  bit-identical to 0 (the reference's lists:
+                                  every tile of the rectangle); the per-item
+                                  counts, keys and tile ranges of those steps
+                                  are the shorter lists.  Renders, forward
+                                  passes and the reference backward mode
+                                  always list every tile.  Default 0.        */
 } SkyConfig;
 
 typedef struct SkyStepStats {

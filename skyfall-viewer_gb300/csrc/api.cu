@@ -516,6 +516,11 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   sp.icap = c->icap;
   sp.num_pixels = (uint32_t)pix_total;
   sp.plane_stride = c->stride;
+  // renders and forward passes keep the reference's lists (the multi-view
+  // scores walk a render's lists), and so does the reference-mode backward:
+  // its batches of 64 list entries set where each pixel's walk restarts, so
+  // its sums depend on the list, not only on the contributing entries
+  sp.tile_cull = (cfg.tile_cull && mode >= kBackward && !ref) ? 1u : 0u;
   sp.near_plane = cfg.near_plane;
   sp.far_plane = cfg.far_plane;
   sp.radius_clip = cfg.radius_clip;
@@ -1055,6 +1060,7 @@ static int check_cfg(const SkyConfig* cfg) {
     return fail(SKY_ERR_ARG, "fwd_batch %u not in {0, 64, 128, 256}", cfg->fwd_batch);
   if (cfg->bwd_batch != 0 && cfg->bwd_batch != 32 && cfg->bwd_batch != 64 && cfg->bwd_batch != 128)
     return fail(SKY_ERR_ARG, "bwd_batch %u not in {0, 32, 64, 128}", cfg->bwd_batch);
+  if (cfg->tile_cull > 1) return fail(SKY_ERR_ARG, "tile_cull %u not 0 or 1", cfg->tile_cull);
   return SKY_OK;
 }
 

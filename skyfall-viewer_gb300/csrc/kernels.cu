@@ -46,10 +46,126 @@ SKY_DEV uint32_t depth_key(float depth) {
   return wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
 }
 
+// Exact test of a splat's raster pre-filter against a rectangle of pixel
+// centres: whether s = 0.5 (a dx^2 + c dy^2) + b dx dy exceeds smax at every
+// centre, so that no pixel there can pass.  dx runs over [u0, u1] = the f32
+// values px - mx of the rectangle's first and last columns (the rasterisers'
+// own dx, monotone in px), dy likewise; the minimum of the convex s over that
+// rectangle lies on one of its edges (or is 0 when it holds the mean): along
+// an edge u = u0 it is at v = -b u0 / c clamped to [v0, v1].  Rounding: for a
+// conic with b^2 <= 0.98 a c, |a dx^2| + |c dy^2| + 2 |b dx dy| <= 400 s, so
+// an f32 evaluation of s (the rasterisers' and this one) is within 3e-4 s of
+// the exact value; the test answers yes only when the computed minimum
+// exceeds 1.001 smax.
+struct EllipseBound {
+  float mx, my, a, b, c;
+  float ku, kv;  // edge minimisers per unit offset, -b/c and -b/a
+  float lim;     // 1.001 smax
+};
+
+// false (no test possible) unless a, c > 0, b^2 <= 0.98 a c and smax > 0.
+// An error in ku, kv only moves a point along its edge, raising s there by a
+// relative O(ulp^2), so the approximate division is enough.
+SKY_DEV bool ellipse_bound(float mx, float my, float a, float bq, float c, float smax,
+                           EllipseBound& e) {
+  if (!(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c)) || !(smax > 0.0f)) return false;
+  e = EllipseBound{mx, my, a, bq, c, -__fdividef(bq, c), -__fdividef(bq, a), 1.001f * smax};
+  return true;
+}
+
+// The rectangle's first pixel centre is (cx, cy) = (x + 0.5, y + 0.5); it is
+// w1 + 1 columns wide and h1 + 1 rows high.
+SKY_DEV bool ellipse_misses(const EllipseBound& e, float cx, float cy, float w1, float h1) {
+  const float u0 = cx - e.mx, u1 = (cx + w1) - e.mx;
+  const float v0 = cy - e.my, v1 = (cy + h1) - e.my;
+  if (u0 <= 0.0f && u1 >= 0.0f && v0 <= 0.0f && v1 >= 0.0f) return false;
+  auto s_at = [&](float u, float v) { return 0.5f * ((e.a * u) * u + (e.c * v) * v) + (e.b * u) * v; };
+  float smin = s_at(u0, fminf(fmaxf(e.ku * u0, v0), v1));
+  smin = fminf(smin, s_at(u1, fminf(fmaxf(e.ku * u1, v0), v1)));
+  smin = fminf(smin, s_at(fminf(fmaxf(e.kv * v0, u0), u1), v0));
+  smin = fminf(smin, s_at(fminf(fmaxf(e.kv * v1, u0), u1), v1));
+  return smin > e.lim;
+}
+
+// Tiles of an item's rectangle (packed as in b.rects).
+SKY_DEV uint32_t rect_area(uint2 rc) {
+  const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
+  return (x1 <= x0 || y1 <= y0) ? 0u : (x1 - x0) * (y1 - y0);
+}
+
+// The ellipse E = {s <= L}, L = 1.001 smax, row by row, for the tile lists:
+// relative to the mean, its rows span |v| <= V = sqrt(2 a L / det)
+// (det = a c - b^2), its rightmost point is (U, -b U / c) with
+// U = sqrt(2 c L / det) (the leftmost the mirror image), and at height v it
+// spans u in [(-b v - sqrt(D)) / a, (-b v + sqrt(D)) / a], D = 2 a L - det v^2.
+// Every pixel that passes the rasterisers' f32 pre-filter has its f32 offsets
+// (dx, dy) inside E (the rounding bound of EllipseBound).
+struct EllipseRows {
+  float mx, my, a, b, det, two_a_l;
+  float V, v_margin;  // V, and 1.01 V + 0.05: the rows listed
+  float u_margin;     // 0.01 U + 0.05, added to each row's extent
+  float v_right;      // -b U / c
+};
+
+SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float smax, EllipseRows& r) {
+  if (!(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c)) || !(smax > 0.0f)) return false;
+  const float L = 1.001f * smax;
+  const float det = a * c - bq * bq;
+  const float U = sqrtf(2.0f * c * L / det);
+  r.mx = mx;
+  r.my = my;
+  r.a = a;
+  r.b = bq;
+  r.det = det;
+  r.two_a_l = 2.0f * a * L;
+  r.V = sqrtf(r.two_a_l / det);
+  r.v_margin = 1.01f * r.V + 0.05f;
+  r.u_margin = 0.01f * U + 0.05f;
+  r.v_right = -bq * U / c;
+  return true;
+}
+
+// Row ty's listed tiles [lo, lo + len) of the rectangle [x0, x1): those
+// whose pixel-centre columns meet E's extent within the row's band of
+// pixel-centre rows [v0, v1] (the rasterisers' own f32 dy at the band's first
+// and last rows).  Over the band the right edge (-b v + sqrt(D)) / a is
+// concave in v, so its maximum is at v_right clamped into the band, and the
+// left edge's minimum at -v_right clamped likewise.  f32 error: det carries
+// up to 6e-6 relative error (b^2 <= 0.98 a c), so D is within 6.2e-6 (2 a L)
+// and each extent within 2.5e-3 U of the exact one; V within 1e-5 V.  The
+// margins (1 % plus 0.05 px) cover that with room, so every tile holding a
+// pixel that can pass the pre-filter is listed; a tile listed in excess only
+// costs time.
+SKY_DEV uint32_t row_span(const EllipseRows& r, uint32_t ty, uint32_t x0, uint32_t x1, uint32_t ts,
+                          uint32_t& lo) {
+  lo = x0;
+  const float cy = (float)(ty * ts) + 0.5f;
+  const float v0 = cy - r.my, v1 = (cy + (float)(ts - 1u)) - r.my;
+  if (v1 < -r.v_margin || v0 > r.v_margin) return 0u;
+  const float w0 = fmaxf(v0, -r.V), w1 = fminf(v1, r.V);
+  const float vr = fminf(fmaxf(r.v_right, w0), w1), vl = fminf(fmaxf(-r.v_right, w0), w1);
+  const float dr = fmaxf(r.two_a_l - r.det * vr * vr, 0.0f);
+  const float dl = fmaxf(r.two_a_l - r.det * vl * vl, 0.0f);
+  const float ur = (-r.b * vr + sqrtf(dr)) / r.a + r.u_margin;
+  const float ul = (-r.b * vl - sqrtf(dl)) / r.a - r.u_margin;
+  // tiles whose centre columns [tx ts + 0.5, tx ts + ts - 0.5] meet [mx + ul, mx + ur]
+  const float fts = (float)ts;
+  const float t_lo = ceilf(((r.mx + ul) - (fts - 0.5f)) / fts);
+  const float t_hi = floorf(((r.mx + ur) - 0.5f) / fts);
+  const float flo = fmaxf(t_lo, (float)x0), fhi = fminf(t_hi, (float)x1 - 1.0f);
+  if (!(fhi >= flo)) return 0u;
+  lo = (uint32_t)flo;
+  return (uint32_t)fhi - lo + 1u;
+}
+
 // Writes the raster record, depth/radius, tile count, rectangle and item sort
 // key (min(count, 0xFFFF) << 16) | depth16 of one item (the sort orders by the
 // depth field; the count rides along for the scan in emission order);
-// smax_g = alpha_skip_bound(o.opacity), the same for every view.
+// smax_g = alpha_skip_bound(o.opacity), the same for every view.  With
+// tile_cull the count is that of the rectangle's tiles in the row spans of
+// the splat's ellipse (row_span; all of them for a conic the test cannot
+// bound, none when smax <= 0), and k_emit lists those same tiles; the
+// rectangle is kept.
 SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, float smax_g,
                               size_t item) {
   // Raster pre-filter: a pair with s > smax has opacity * exp(-s) < 1/255
@@ -73,10 +189,22 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
   rec[0] = make_float4(o.mx, o.my, o.ca, o.cb);
   rec[1] = make_float4(o.cc, o.opacity, o.col[0], o.col[1]);
   rec[2] = make_float4(o.col[2], smax, hx, hy);
+  uint32_t count = o.count;
+  const StepParams& sp = *b.sp;
+  if (sp.tile_cull && count > 0u) {
+    EllipseRows e;
+    if (!(smax > 0.0f)) {
+      count = 0u;
+    } else if (ellipse_rows(o.mx, o.my, o.ca, o.cb, o.cc, smax, e)) {
+      count = 0u;
+      uint32_t lo;
+      for (uint32_t ty = o.y0; ty < o.y1; ++ty) count += row_span(e, ty, o.x0, o.x1, sp.tile_size, lo);
+    }
+  }
   b.aux[item] = make_float2(o.depth, o.radius);
-  b.counts[item] = o.count;
+  b.counts[item] = count;
   b.rects[item] = make_uint2(o.x0 | (o.y0 << 16), o.x1 | (o.y1 << 16));
-  b.ikeys[item] = (min(o.count, 0xFFFFu) << 16) | depth_key(o.depth);
+  b.ikeys[item] = (min(count, 0xFFFFu) << 16) | depth_key(o.depth);
 }
 
 // ---------------------------------------------------------------------------
@@ -238,11 +366,13 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const uint32_t pos = v * sp.n + g;  // position in emission (perm) order
   // items of one sort group's views interleave: the view is the item's own;
   // the sorted item key carries its depth field
-  uint32_t item, view, dq;
+  uint32_t item, view, dq, c16 = 0xFFFFu;
   if (b.perm) {
     item = b.perm[pos];
     view = item / sp.n;
-    dq = b.ikeys_sorted[pos] & 0xFFFFu;
+    const uint32_t ik = b.ikeys_sorted[pos];
+    dq = ik & 0xFFFFu;
+    c16 = ik >> 16;
   } else {
     item = pos;
     view = v;
@@ -250,20 +380,51 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   }
   const uint2 rc = b.rects[item];
   const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
-  if (x1 <= x0 || y1 <= y0) return;  // no tiles (the count is the rectangle's area)
-  const uint32_t cnt = (x1 - x0) * (y1 - y0);
+  if (x1 <= x0 || y1 <= y0) return;  // no tiles
+  const uint32_t area = (x1 - x0) * (y1 - y0);
+  // the count is the rectangle's area unless the lists are culled (then the
+  // sorted item key carries it when below 0xFFFF)
+  const uint32_t cnt = !sp.tile_cull ? area : (c16 < 0xFFFFu ? c16 : b.counts[item]);
+  if (cnt == 0u) return;
   const uint32_t end = b.cumsum[pos];
   if (end > sp.icap) return;
   uint32_t cur = end - cnt;
   const ViewInfo& vi = sp.views[view];
   const uint32_t it = item;
-  for (uint32_t ty = y0; ty < y1; ++ty)
-    for (uint32_t tx = x0; tx < x1; ++tx) {
+  if (cnt == area) {
+    for (uint32_t ty = y0; ty < y1; ++ty)
+      for (uint32_t tx = x0; tx < x1; ++tx) {
+        const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
+        b.keys[cur] = (kt << 16) | dq;
+        b.rec_of[cur] = it;
+        ++cur;
+      }
+    return;
+  }
+  // culled: the tiles the preprocess counted, by the same test on the same
+  // record values
+  const float4 r0 = b.records[(size_t)item * 3 + 0];
+  const float cc = b.records[(size_t)item * 3 + 1].x, smax = b.records[(size_t)item * 3 + 2].y;
+  EllipseRows e;
+  if (!ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
+    atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);  // counted differently: corrupt lists
+    return;
+  }
+  for (uint32_t ty = y0; ty < y1; ++ty) {
+    uint32_t lo;
+    const uint32_t len = row_span(e, ty, x0, x1, sp.tile_size, lo);
+    if (len > end - cur) {
+      atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);
+      return;
+    }
+    for (uint32_t tx = lo; tx < lo + len; ++tx) {
       const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
       b.keys[cur] = (kt << 16) | dq;
       b.rec_of[cur] = it;
       ++cur;
     }
+  }
+  if (cur != end) atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);
 }
 
 // ---------------------------------------------------------------------------
@@ -354,41 +515,20 @@ SKY_DEV uint32_t block_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
 }
 
 // block_mask with the bounding box replaced, block by block, by the ellipse
-// itself: bit w is cleared when s = 0.5 (a dx^2 + c dy^2) + b dx dy exceeds
-// smax at every pixel centre of block w, so no pixel there can pass the
-// raster pre-filter and the block's warp would do nothing with the splat.
-// Per block, dx runs over [u0, u1] = the f32 values px - mx of the block's
-// first and last columns (the kernels' own dx, monotone in px), dy likewise;
-// the minimum of the convex s over that rectangle lies on one of its edges
-// (or is 0 when the rectangle holds the mean): along an edge u = u0 it is at
-// v = -b u0 / c clamped to [v0, v1].  Rounding: for a conic with
-// b^2 <= 0.98 a c, |a dx^2| + |c dy^2| + 2 |b dx dy| <= 400 s, so an f32
-// evaluation of s (the kernels' and this one) is within 3e-4 s of the exact
-// value; a block is dropped only when the computed minimum exceeds
-// 1.001 smax.  Worse-conditioned conics keep the bounding-box mask.
+// itself (ellipse_misses): bit w is cleared when no pixel of block w can
+// pass the raster pre-filter, so the block's warp would do nothing with the
+// splat.  Worse-conditioned conics keep the bounding-box mask.
 template <int TS, int BW, int BH>
 SKY_DEV uint32_t ellipse_mask(float4 r0, float4 r1, float4 r2, uint32_t x0, uint32_t y0) {
   constexpr int NCOL = TS / BW;
   uint32_t m = block_mask<TS, BW, BH>(r0, r2, x0, y0);
-  const float a = r0.z, bq = r0.w, c = r1.x;
-  if (m == 0u || !(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c))) return m;
-  const float lim = 1.001f * r2.y;
-  // edge minimisers per unit offset; an error in them only moves the point
-  // along the edge, raising s there by a relative O(ulp^2)
-  const float ku = -__fdividef(bq, c), kv = -__fdividef(bq, a);
-  auto s_at = [&](float u, float v) { return 0.5f * ((a * u) * u + (c * v) * v) + (bq * u) * v; };
+  EllipseBound e;
+  if (m == 0u || !ellipse_bound(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
   for (uint32_t rest = m; rest != 0u; rest &= rest - 1u) {
     const int w = __ffs(rest) - 1;
     const float cx = (float)(x0 + (uint32_t)((w % NCOL) * BW)) + 0.5f;
     const float cy = (float)(y0 + (uint32_t)((w / NCOL) * BH)) + 0.5f;
-    const float u0 = cx - r0.x, u1 = (cx + (float)(BW - 1)) - r0.x;
-    const float v0 = cy - r0.y, v1 = (cy + (float)(BH - 1)) - r0.y;
-    if (u0 <= 0.0f && u1 >= 0.0f && v0 <= 0.0f && v1 >= 0.0f) continue;
-    float smin = s_at(u0, fminf(fmaxf(ku * u0, v0), v1));
-    smin = fminf(smin, s_at(u1, fminf(fmaxf(ku * u1, v0), v1)));
-    smin = fminf(smin, s_at(fminf(fmaxf(kv * v0, u0), u1), v0));
-    smin = fminf(smin, s_at(fminf(fmaxf(kv * v1, u0), u1), v1));
-    if (smin > lim) m &= ~(1u << w);
+    if (ellipse_misses(e, cx, cy, (float)(BW - 1), (float)(BH - 1))) m &= ~(1u << w);
   }
   return m;
 }
@@ -1551,8 +1691,11 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
       imp.x = imp.x * sp.importance_decay;
       imp.y = imp.y * sp.importance_decay;
       imp.z = imp.z * sp.importance_decay;
-      if (cnt > 0u) {
-        imp.x = imp.x + (float)cnt;
+      // the statistic counts the tiles of the item's rectangle, also when
+      // the intersection lists hold only the tiles its ellipse reaches
+      const uint32_t tiles = sp.tile_cull ? rect_area(b.rects[item]) : cnt;
+      if (tiles > 0u) {
+        imp.x = imp.x + (float)tiles;
         imp.y = imp.y + 1.0f;
         imp.z = fmax_(imp.z, s_aux[buf][t].y);
       }

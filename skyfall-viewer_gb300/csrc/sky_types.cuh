@@ -44,7 +44,8 @@ struct StepParams {
   uint32_t num_views, n, num_tiles, num_groups;
   uint32_t sh_deg, sh_update, bwd_mode, round_f16;
   uint32_t tile_size, has_loss, apply_adam, write_grads;
-  uint32_t icap, num_pixels, plane_stride, pad0;
+  uint32_t icap, num_pixels, plane_stride;
+  uint32_t tile_cull;  // 1: items list only the tiles their alpha >= 1/255 ellipse reaches
   float near_plane, far_plane, radius_clip, eps2d;
   float bg[4];
   float w_l2, w_l1, w_ssim, pad1;

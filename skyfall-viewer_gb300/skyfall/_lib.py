@@ -73,7 +73,7 @@ class SkyConfig(C.Structure):
         ("beta2", C.c_float), ("adam_eps", C.c_float), ("sh_update_interval", C.c_uint32),
         ("round_params_f16", C.c_uint32), ("backward_mode", C.c_uint32), ("use_graph", C.c_uint32),
         ("max_views_per_step", C.c_uint32), ("seed", C.c_uint64),
-        ("fwd_batch", C.c_uint32), ("bwd_batch", C.c_uint32),
+        ("fwd_batch", C.c_uint32), ("bwd_batch", C.c_uint32), ("tile_cull", C.c_uint32),
     ]
 
 

@@ -330,6 +330,14 @@ class GaussianRenderer:
         self.config.bwd_batch = bwd_batch
         L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
 
+    def setTileCull(self, on: bool) -> None:
+        """Intersection lists of backward and training steps limited to the
+        tiles each Gaussian's alpha >= 1/255 ellipse reaches (exact: images,
+        loss, gradients and parameters are bit-identical either way; renders
+        keep every tile of the rectangle)."""
+        self.config.tile_cull = 1 if on else 0
+        L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
+
     def getLossWeights(self) -> LossWeights:
         return LossWeights(self.config.w_l2, self.config.w_l1, self.config.w_ssim)
 
