@@ -1,18 +1,20 @@
-"""The backward's per-block ellipse test, checked on the CPU (no GPU).
+"""The ellipse tests that skip work, checked on the CPU (no GPU).
 
 Before the exact backward walks a batch of splats, each splat's bounding-box
 block mask is narrowed block by block: an 8x8 pixel block is dropped when the
 minimum of s = 0.5 (a dx^2 + c dy^2) + b dx dy over the block's rectangle of
 pixel centres, evaluated in f32 along the rectangle's edges, exceeds
-1.001 smax.  Dropping a block that holds a pixel with f32 s <= smax would
-lose that pixel's contribution.  This test restates the test's f32
-arithmetic (ellipse_mask in kernels.cu) in numpy, one rounding per
-operation, and checks it against the kernels' own f32 evaluation of s at
-every pixel centre of the block, on random splats with anisotropy up to the
-test's conditioning limit (b^2 <= 0.98 a c) and means on both sides of the
-block's edges.
+1.001 smax.  With culled intersection lists, each tile row of a Gaussian's
+rectangle lists only the tiles that meet the analytic extent of that ellipse
+within the row.  Dropping a block or tile that holds a pixel with f32
+s <= smax would lose that pixel's contribution.  These tests restate the f32
+arithmetic (ellipse_mask and row_span in kernels.cu) in numpy, one rounding
+per operation, and check it against the rasterisers' own f32 evaluation of s
+at every pixel centre, on random splats with anisotropy up to the tests'
+conditioning limit (b^2 <= 0.98 a c) and means on both sides of the edges.
 """
 import numpy as np
+import pytest
 
 f = np.float32
 
@@ -86,6 +88,67 @@ def test_dropped_blocks_hold_no_pixel_within_smax():
         assert drop.sum() >= 0.95 * (live & ~reach).sum()
         total_dropped += int(drop.sum())
     assert total_dropped > 50000
+
+
+def row_span(a, b, c, mx, my, smax, ty, x0, x1, ts):
+    """row_span (kernels.cu) in f32: the listed tiles [lo, lo + len) of tile
+    row ty of the rectangle [x0, x1)."""
+    L = f(1.001) * smax
+    det = a * c - b * b
+    U = np.sqrt(f(2) * c * L / det)
+    two_a_l = f(2) * a * L
+    V = np.sqrt(two_a_l / det)
+    v_margin = f(1.01) * V + f(0.05)
+    u_margin = f(0.01) * U + f(0.05)
+    v_right = -b * U / c
+    cy = f(ty * ts) + f(0.5)
+    v0 = cy - my
+    v1 = (cy + f(ts - 1)) - my
+    if v1 < -v_margin or v0 > v_margin:
+        return x0, 0
+    w0, w1 = max(v0, -V), min(v1, V)
+    vr, vl = min(max(v_right, w0), w1), min(max(-v_right, w0), w1)
+    dr = max(two_a_l - det * vr * vr, f(0))
+    dl = max(two_a_l - det * vl * vl, f(0))
+    ur = (-b * vr + np.sqrt(dr)) / a + u_margin
+    ul = (-b * vl - np.sqrt(dl)) / a - u_margin
+    fts = f(ts)
+    t_lo = np.ceil(((mx + ul) - (fts - f(0.5))) / fts)
+    t_hi = np.floor(((mx + ur) - f(0.5)) / fts)
+    flo, fhi = max(t_lo, f(x0)), min(t_hi, f(x1 - 1))
+    if not fhi >= flo:
+        return x0, 0
+    return int(flo), int(fhi) - int(flo) + 1
+
+
+@pytest.mark.parametrize("ts", [8, 16, 32])
+def test_row_spans_list_every_reached_tile(ts):
+    """The culled intersection lists: per tile row of a Gaussian's rectangle,
+    the analytic span of its ellipse must hold every tile with a pixel whose
+    f32 s passes the pre-filter, and list few tiles beyond those."""
+    rng = np.random.default_rng(20 + ts)
+    a, b, c, mx, my, smax = random_splats(rng, 1500, 1000, 500)
+    l_max = np.maximum(1.0 / a, 1.0 / c) * 4.0  # generous radius for the rectangle
+    reached = listed = 0
+    for i in range(a.size):
+        if not (smax[i] > 0 and b[i] * b[i] <= f(0.98) * (a[i] * c[i])):
+            continue
+        rad = int(np.ceil(3 * np.sqrt(l_max[i])))
+        x0, x1 = int(np.floor((mx[i] - rad) / ts)), int(np.ceil((mx[i] + rad) / ts))
+        y0, y1 = int(np.floor((my[i] - rad) / ts)), int(np.ceil((my[i] + rad) / ts))
+        for ty in range(y0, y1):
+            lo, n = row_span(a[i], b[i], c[i], mx[i], my[i], smax[i], ty, x0, x1, ts)
+            listed += n
+            ys = f(ty * ts) + f(0.5) + np.arange(ts, dtype=f)
+            for tx in range(x0, x1):
+                xs = f(tx * ts) + f(0.5) + np.arange(ts, dtype=f)
+                X, Y = np.meshgrid(xs, ys)
+                s = kernel_s(a[i], b[i], c[i], mx[i], my[i], X, Y)
+                if ((s >= 0) & (s <= smax[i])).any():
+                    reached += 1
+                    assert lo <= tx < lo + n, (i, ty, tx, lo, n)
+    assert reached > 1000
+    assert listed <= 1.1 * reached
 
 
 def test_ill_conditioned_conics_are_never_dropped():
