@@ -1044,7 +1044,7 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
   }
   const float a = fmin_(al, MAX_ALPHA);
   if (!(a >= MIN_ALPHA)) return false;
-  const float om = fmax_(1.0f - a, 0.0001f);
+  const float om = 1.0f - a;  // >= 0.001 (a <= 0.999): the reference's max(1 - a, 1e-4)
   const float Tb = __fdividef(p.T, om);
   const float ctb = a * Tb;
   const float d0 = q1.z - p.acc[0], d1 = q1.w - p.acc[1], d2 = q2.x - p.acc[2];
