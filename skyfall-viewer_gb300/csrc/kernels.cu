@@ -46,60 +46,23 @@ SKY_DEV uint32_t depth_key(float depth) {
   return wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
 }
 
-// Exact test of a splat's raster pre-filter against a rectangle of pixel
-// centres: whether s = 0.5 (a dx^2 + c dy^2) + b dx dy exceeds smax at every
-// centre, so that no pixel there can pass.  dx runs over [u0, u1] = the f32
-// values px - mx of the rectangle's first and last columns (the rasterisers'
-// own dx, monotone in px), dy likewise; the minimum of the convex s over that
-// rectangle lies on one of its edges (or is 0 when it holds the mean): along
-// an edge u = u0 it is at v = -b u0 / c clamped to [v0, v1].  Rounding: for a
-// conic with b^2 <= 0.98 a c, |a dx^2| + |c dy^2| + 2 |b dx dy| <= 400 s, so
-// an f32 evaluation of s (the rasterisers' and this one) is within 3e-4 s of
-// the exact value; the test answers yes only when the computed minimum
-// exceeds 1.001 smax.
-struct EllipseBound {
-  float mx, my, a, b, c;
-  float ku, kv;  // edge minimisers per unit offset, -b/c and -b/a
-  float lim;     // 1.001 smax
-};
-
-// false (no test possible) unless a, c > 0, b^2 <= 0.98 a c and smax > 0.
-// An error in ku, kv only moves a point along its edge, raising s there by a
-// relative O(ulp^2), so the approximate division is enough.
-SKY_DEV bool ellipse_bound(float mx, float my, float a, float bq, float c, float smax,
-                           EllipseBound& e) {
-  if (!(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c)) || !(smax > 0.0f)) return false;
-  e = EllipseBound{mx, my, a, bq, c, -__fdividef(bq, c), -__fdividef(bq, a), 1.001f * smax};
-  return true;
-}
-
-// The rectangle's first pixel centre is (cx, cy) = (x + 0.5, y + 0.5); it is
-// w1 + 1 columns wide and h1 + 1 rows high.
-SKY_DEV bool ellipse_misses(const EllipseBound& e, float cx, float cy, float w1, float h1) {
-  const float u0 = cx - e.mx, u1 = (cx + w1) - e.mx;
-  const float v0 = cy - e.my, v1 = (cy + h1) - e.my;
-  if (u0 <= 0.0f && u1 >= 0.0f && v0 <= 0.0f && v1 >= 0.0f) return false;
-  auto s_at = [&](float u, float v) { return 0.5f * ((e.a * u) * u + (e.c * v) * v) + (e.b * u) * v; };
-  float smin = s_at(u0, fminf(fmaxf(e.ku * u0, v0), v1));
-  smin = fminf(smin, s_at(u1, fminf(fmaxf(e.ku * u1, v0), v1)));
-  smin = fminf(smin, s_at(fminf(fmaxf(e.kv * v0, u0), u1), v0));
-  smin = fminf(smin, s_at(fminf(fmaxf(e.kv * v1, u0), u1), v1));
-  return smin > e.lim;
-}
-
 // Tiles of an item's rectangle (packed as in b.rects).
 SKY_DEV uint32_t rect_area(uint2 rc) {
   const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
   return (x1 <= x0 || y1 <= y0) ? 0u : (x1 - x0) * (y1 - y0);
 }
 
-// The ellipse E = {s <= L}, L = 1.001 smax, row by row, for the tile lists:
-// relative to the mean, its rows span |v| <= V = sqrt(2 a L / det)
-// (det = a c - b^2), its rightmost point is (U, -b U / c) with
-// U = sqrt(2 c L / det) (the leftmost the mirror image), and at height v it
-// spans u in [(-b v - sqrt(D)) / a, (-b v + sqrt(D)) / a], D = 2 a L - det v^2.
-// Every pixel that passes the rasterisers' f32 pre-filter has its f32 offsets
-// (dx, dy) inside E (the rounding bound of EllipseBound).
+// The ellipse E = {s <= L}, L = 1.001 smax, of a splat's raster pre-filter
+// s = 0.5 (a dx^2 + c dy^2) + b dx dy <= smax, row by row, to skip tiles and
+// pixel blocks where no pixel can pass it.  Relative to the mean, E's rows
+// span |v| <= V = sqrt(2 a L / det) (det = a c - b^2), its rightmost point is
+// (U, -b U / c) with U = sqrt(2 c L / det) (the leftmost the mirror image),
+// and at height v it spans u in [(-b v - sqrt(D)) / a, (-b v + sqrt(D)) / a],
+// D = 2 a L - det v^2.  Rounding: for a conic with b^2 <= 0.98 a c,
+// |a dx^2| + |c dy^2| + 2 |b dx dy| <= 400 s, so the rasterisers' f32
+// evaluation of s is within 3e-4 s of the exact value at their f32 offsets
+// (dx, dy): every pixel that passes the pre-filter has those offsets inside E.
+// Worse-conditioned conics (and smax <= 0) get no EllipseRows.
 struct EllipseRows {
   float mx, my, a, b, det, two_a_l;
   float V, v_margin;  // V, and 1.01 V + 0.05: the rows listed
@@ -125,29 +88,37 @@ SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float 
   return true;
 }
 
+// E's extent [ul, ur] (relative to the mean, margins included) within a band
+// of pixel-centre rows whose f32 dy run over [v0, v1] (the rasterisers' own
+// dy at the band's first and last rows); false when the band misses E.  Over
+// the band the right edge (-b v + sqrt(D)) / a is concave in v, so its
+// maximum is at v_right clamped into the band, and the left edge's minimum at
+// -v_right clamped likewise.  f32 error: det carries up to 6e-6 relative
+// error (b^2 <= 0.98 a c), so D is within 6.2e-6 (2 a L) and each extent
+// within 2.5e-3 U of the exact one; V within 1e-5 V.  The margins (1 % plus
+// 0.05 px) cover that with room, so a pixel column outside [mx + ul, mx + ur]
+// holds no pixel of the band that can pass the pre-filter; a column kept in
+// excess only costs time.
+SKY_DEV bool band_extent(const EllipseRows& r, float v0, float v1, float& ul, float& ur) {
+  if (v1 < -r.v_margin || v0 > r.v_margin) return false;
+  const float w0 = fmaxf(v0, -r.V), w1 = fminf(v1, r.V);
+  const float vr = fminf(fmaxf(r.v_right, w0), w1), vl = fminf(fmaxf(-r.v_right, w0), w1);
+  const float dr = fmaxf(r.two_a_l - r.det * vr * vr, 0.0f);
+  const float dl = fmaxf(r.two_a_l - r.det * vl * vl, 0.0f);
+  ur = (-r.b * vr + sqrtf(dr)) / r.a + r.u_margin;
+  ul = (-r.b * vl - sqrtf(dl)) / r.a - r.u_margin;
+  return true;
+}
+
 // Row ty's listed tiles [lo, lo + len) of the rectangle [x0, x1): those
-// whose pixel-centre columns meet E's extent within the row's band of
-// pixel-centre rows [v0, v1] (the rasterisers' own f32 dy at the band's first
-// and last rows).  Over the band the right edge (-b v + sqrt(D)) / a is
-// concave in v, so its maximum is at v_right clamped into the band, and the
-// left edge's minimum at -v_right clamped likewise.  f32 error: det carries
-// up to 6e-6 relative error (b^2 <= 0.98 a c), so D is within 6.2e-6 (2 a L)
-// and each extent within 2.5e-3 U of the exact one; V within 1e-5 V.  The
-// margins (1 % plus 0.05 px) cover that with room, so every tile holding a
-// pixel that can pass the pre-filter is listed; a tile listed in excess only
-// costs time.
+// whose pixel-centre columns meet E's extent within the row's band.
 SKY_DEV uint32_t row_span(const EllipseRows& r, uint32_t ty, uint32_t x0, uint32_t x1, uint32_t ts,
                           uint32_t& lo) {
   lo = x0;
   const float cy = (float)(ty * ts) + 0.5f;
   const float v0 = cy - r.my, v1 = (cy + (float)(ts - 1u)) - r.my;
-  if (v1 < -r.v_margin || v0 > r.v_margin) return 0u;
-  const float w0 = fmaxf(v0, -r.V), w1 = fminf(v1, r.V);
-  const float vr = fminf(fmaxf(r.v_right, w0), w1), vl = fminf(fmaxf(-r.v_right, w0), w1);
-  const float dr = fmaxf(r.two_a_l - r.det * vr * vr, 0.0f);
-  const float dl = fmaxf(r.two_a_l - r.det * vl * vl, 0.0f);
-  const float ur = (-r.b * vr + sqrtf(dr)) / r.a + r.u_margin;
-  const float ul = (-r.b * vl - sqrtf(dl)) / r.a - r.u_margin;
+  float ul, ur;
+  if (!band_extent(r, v0, v1, ul, ur)) return 0u;
   // tiles whose centre columns [tx ts + 0.5, tx ts + ts - 0.5] meet [mx + ul, mx + ur]
   const float fts = (float)ts;
   const float t_lo = ceilf(((r.mx + ul) - (fts - 0.5f)) / fts);
@@ -514,23 +485,33 @@ SKY_DEV uint32_t block_mask(float4 r0, float4 r2, uint32_t x0, uint32_t y0) {
   return mask;
 }
 
-// block_mask with the bounding box replaced, block by block, by the ellipse
-// itself (ellipse_misses): bit w is cleared when no pixel of block w can
-// pass the raster pre-filter, so the block's warp would do nothing with the
-// splat.  Worse-conditioned conics keep the bounding-box mask.
+// block_mask with the bounding box replaced by the ellipse itself, band by
+// band (band_extent): per row of BW x BH blocks, E's x-extent within the
+// row's BH pixel rows, and block c kept when its pixel-centre columns meet
+// it.  A cleared bit means no pixel of the block can pass the raster
+// pre-filter, so the block's warp would do nothing with the splat.
+// Worse-conditioned conics keep the bounding-box mask.
 template <int TS, int BW, int BH>
-SKY_DEV uint32_t ellipse_mask(float4 r0, float4 r1, float4 r2, uint32_t x0, uint32_t y0) {
-  constexpr int NCOL = TS / BW;
-  uint32_t m = block_mask<TS, BW, BH>(r0, r2, x0, y0);
-  EllipseBound e;
-  if (m == 0u || !ellipse_bound(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
-  for (uint32_t rest = m; rest != 0u; rest &= rest - 1u) {
-    const int w = __ffs(rest) - 1;
-    const float cx = (float)(x0 + (uint32_t)((w % NCOL) * BW)) + 0.5f;
-    const float cy = (float)(y0 + (uint32_t)((w / NCOL) * BH)) + 0.5f;
-    if (ellipse_misses(e, cx, cy, (float)(BW - 1), (float)(BH - 1))) m &= ~(1u << w);
+SKY_DEV uint32_t ellipse_band_mask(float4 r0, float4 r1, float4 r2, uint32_t x0, uint32_t y0) {
+  constexpr int NCOL = TS / BW, NROW = TS / BH;
+  const uint32_t m = block_mask<TS, BW, BH>(r0, r2, x0, y0);
+  EllipseRows e;
+  if (m == 0u || !ellipse_rows(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
+  uint32_t keep = 0u;
+#pragma unroll 1
+  for (int br = 0; br < NROW; ++br) {
+    if (((m >> (br * NCOL)) & ((1u << NCOL) - 1u)) == 0u) continue;
+    const float cy = (float)(y0 + (uint32_t)(br * BH)) + 0.5f;
+    float ul, ur;
+    if (!band_extent(e, cy - e.my, (cy + (float)(BH - 1)) - e.my, ul, ur)) continue;
+    const float xl = e.mx + ul, xr = e.mx + ur;
+#pragma unroll
+    for (int bc = 0; bc < NCOL; ++bc) {
+      const float cx = (float)(x0 + (uint32_t)(bc * BW)) + 0.5f;
+      if (xr >= cx && xl <= cx + (float)(BW - 1)) keep |= 1u << (br * NCOL + bc);
+    }
   }
-  return m;
+  return m & keep;
 }
 
 template <int TS, int RPW = 32 / TS>
@@ -1138,7 +1119,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
       stage_record(s_rec + k * 3, q0, q1, q2);
-      s_mask[k] = ellipse_mask<TS, 8, 8>(q0, q1, q2, tx * TS, ty * TS);
+      s_mask[k] = ellipse_band_mask<TS, 8, 8>(q0, q1, q2, tx * TS, ty * TS);
     }
     __syncthreads();
     uint32_t nlist = 0;

@@ -1,17 +1,18 @@
 """The ellipse tests that skip work, checked on the CPU (no GPU).
 
-Before the exact backward walks a batch of splats, each splat's bounding-box
-block mask is narrowed block by block: an 8x8 pixel block is dropped when the
-minimum of s = 0.5 (a dx^2 + c dy^2) + b dx dy over the block's rectangle of
-pixel centres, evaluated in f32 along the rectangle's edges, exceeds
-1.001 smax.  With culled intersection lists, each tile row of a Gaussian's
-rectangle lists only the tiles that meet the analytic extent of that ellipse
+Both use the analytic x-extent of the ellipse s = 0.5 (a dx^2 + c dy^2) +
+b dx dy <= 1.001 smax within a band of pixel rows.  Before the exact backward
+walks a batch of splats, each splat's bounding-box block mask is narrowed: an
+8x8 pixel block is dropped when its pixel-centre columns miss that extent
+within its 8 rows.  With culled intersection lists, each tile row of a
+Gaussian's rectangle lists only the tiles whose columns meet the extent
 within the row.  Dropping a block or tile that holds a pixel with f32
 s <= smax would lose that pixel's contribution.  These tests restate the f32
-arithmetic (ellipse_mask and row_span in kernels.cu) in numpy, one rounding
-per operation, and check it against the rasterisers' own f32 evaluation of s
-at every pixel centre, on random splats with anisotropy up to the tests'
-conditioning limit (b^2 <= 0.98 a c) and means on both sides of the edges.
+arithmetic (ellipse_rows, band_extent, ellipse_band_mask and row_span in
+kernels.cu) in numpy, one rounding per operation, and check it against the
+rasterisers' own f32 evaluation of s at every pixel centre, on random splats
+with anisotropy up to the conditioning limit (b^2 <= 0.98 a c) and means on
+both sides of the edges.
 """
 import numpy as np
 import pytest
@@ -29,29 +30,39 @@ def kernel_s(a, b, c, mx, my, px, py):
     return so2 + (b * dx) * dy
 
 
+def band_extent(a, b, c, mx, my, smax, v0, v1):
+    """ellipse_rows + band_extent (kernels.cu) in f32, elementwise: whether
+    the band of pixel-centre rows with dy in [v0, v1] meets the ellipse, and
+    its x-extent [ul, ur] relative to the mean there (margins included)."""
+    L = f(1.001) * smax
+    det = a * c - b * b
+    U = np.sqrt(f(2) * c * L / det)
+    two_a_l = f(2) * a * L
+    V = np.sqrt(two_a_l / det)
+    v_margin = f(1.01) * V + f(0.05)
+    u_margin = f(0.01) * U + f(0.05)
+    v_right = -b * U / c
+    meets = ~((v1 < -v_margin) | (v0 > v_margin))
+    w0, w1 = np.maximum(v0, -V), np.minimum(v1, V)
+    vr = np.minimum(np.maximum(v_right, w0), w1)
+    vl = np.minimum(np.maximum(-v_right, w0), w1)
+    dr = np.maximum(two_a_l - det * vr * vr, f(0))
+    dl = np.maximum(two_a_l - det * vl * vl, f(0))
+    ur = (-b * vr + np.sqrt(dr)) / a + u_margin
+    ul = (-b * vl - np.sqrt(dl)) / a - u_margin
+    return meets, ul, ur
+
+
 def block_dropped(a, b, c, mx, my, smax, x0, y0, bw, bh):
-    cond = (a > 0) & (c > 0) & (b * b <= f(0.98) * (a * c))
-    ku = -(b / c)
-    kv = -(b / a)
-
-    def s_at(u, v):
-        return f(0.5) * ((a * u) * u + (c * v) * v) + (b * u) * v
-
-    def clamp(x, lo, hi):
-        return np.minimum(np.maximum(x, lo), hi)
-
-    cx = f(x0) + f(0.5)
-    cy = f(y0) + f(0.5)
-    u0 = cx - mx
-    u1 = (cx + f(bw - 1)) - mx
-    v0 = cy - my
-    v1 = (cy + f(bh - 1)) - my
-    holds_mean = (u0 <= 0) & (u1 >= 0) & (v0 <= 0) & (v1 >= 0)
-    smin = s_at(u0, clamp(ku * u0, v0, v1))
-    smin = np.minimum(smin, s_at(u1, clamp(ku * u1, v0, v1)))
-    smin = np.minimum(smin, s_at(clamp(kv * v0, u0, u1), v0))
-    smin = np.minimum(smin, s_at(clamp(kv * v1, u0, u1), v1))
-    return cond & ~holds_mean & (smin > f(1.001) * smax)
+    """ellipse_band_mask's decision for one bw x bh block at (x0, y0)."""
+    cond = (a > 0) & (c > 0) & (b * b <= f(0.98) * (a * c)) & (smax > 0)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        cy = f(y0) + f(0.5)
+        meets, ul, ur = band_extent(a, b, c, mx, my, smax, cy - my, (cy + f(bh - 1)) - my)
+        xl, xr = mx + ul, mx + ur
+        cx = f(x0) + f(0.5)
+        kept = meets & (xr >= cx) & (xl <= cx + f(bw - 1))
+    return cond & ~kept
 
 
 def random_splats(rng, n, x0, y0):
@@ -93,25 +104,10 @@ def test_dropped_blocks_hold_no_pixel_within_smax():
 def row_span(a, b, c, mx, my, smax, ty, x0, x1, ts):
     """row_span (kernels.cu) in f32: the listed tiles [lo, lo + len) of tile
     row ty of the rectangle [x0, x1)."""
-    L = f(1.001) * smax
-    det = a * c - b * b
-    U = np.sqrt(f(2) * c * L / det)
-    two_a_l = f(2) * a * L
-    V = np.sqrt(two_a_l / det)
-    v_margin = f(1.01) * V + f(0.05)
-    u_margin = f(0.01) * U + f(0.05)
-    v_right = -b * U / c
     cy = f(ty * ts) + f(0.5)
-    v0 = cy - my
-    v1 = (cy + f(ts - 1)) - my
-    if v1 < -v_margin or v0 > v_margin:
+    meets, ul, ur = band_extent(a, b, c, mx, my, smax, cy - my, (cy + f(ts - 1)) - my)
+    if not meets:
         return x0, 0
-    w0, w1 = max(v0, -V), min(v1, V)
-    vr, vl = min(max(v_right, w0), w1), min(max(-v_right, w0), w1)
-    dr = max(two_a_l - det * vr * vr, f(0))
-    dl = max(two_a_l - det * vl * vl, f(0))
-    ur = (-b * vr + np.sqrt(dr)) / a + u_margin
-    ul = (-b * vl - np.sqrt(dl)) / a - u_margin
     fts = f(ts)
     t_lo = np.ceil(((mx + ul) - (fts - f(0.5))) / fts)
     t_hi = np.floor(((mx + ur) - f(0.5)) / fts)
