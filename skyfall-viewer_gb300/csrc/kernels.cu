@@ -1589,8 +1589,10 @@ constexpr size_t kGeomSmem =
 
 // SH values and SH-gradient accumulators live in shared memory (one column
 // per thread, conflict-free), as do the item sums of the next view, copied
-// asynchronously while the current view's adjoint runs; three blocks per
-// multiprocessor resident (168 registers, 60 KB of shared memory each).
+// asynchronously while the current view's adjoint runs, and the step's
+// cameras; three blocks per multiprocessor resident (168 registers, 60 KB of
+// dynamic and 12 KB of static shared memory each).
+static_assert(sizeof(ViewInfo) % 4 == 0, "cameras are copied as 32-bit words");
 __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   extern __shared__ float4 s_dyn[];
   float* const s_base = reinterpret_cast<float*>(s_dyn);
@@ -1601,6 +1603,15 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   float2 (*s_aux)[kGeomThreads] =
       reinterpret_cast<float2 (*)[kGeomThreads]>(s_base + 96 * kGeomThreads + 2 * 3 * kGeomThreads * 4);
   const StepParams& sp = *b.sp;
+  // the step's cameras, read by every thread in every view iteration
+  __shared__ ViewInfo s_views[kMaxViews];
+  {
+    const uint32_t words = sp.num_views * (uint32_t)(sizeof(ViewInfo) / 4);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(sp.views);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_views);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
   if (capacity_failed(b.status)) return;
   const int t = threadIdx.x;
   const uint32_t g = blockIdx.x * blockDim.x + t;
@@ -1720,7 +1731,7 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     // an item with tiles passed the preprocess's culling with these same
     // parameters, so only the camera-space mean, the view direction and the
     // colour are formed again
-    const ViewInfo& vi = sp.views[v];
+    const ViewInfo& vi = s_views[v];
     float pc[4];
     view_position(get, vi, pc);
     ProjOut o;
