@@ -188,7 +188,21 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
 constexpr int kPrepThreads = 128;
 __global__ void __launch_bounds__(kPrepThreads, 8) k_preprocess(DevBuffers b) {
   __shared__ float s_sh[48][kPrepThreads];
+  extern __shared__ ViewInfo s_views[];  // the step's cameras (num_views)
   const StepParams& sp = *b.sp;
+  {
+    uint32_t dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    if (sp.num_views * (uint32_t)sizeof(ViewInfo) > dyn) {  // launched for fewer views
+      if (threadIdx.x == 0) atomicOr(&b.status->error, SKY_DEVERR_CAPACITY);
+      return;
+    }
+    const uint32_t words = sp.num_views * (uint32_t)(sizeof(ViewInfo) / 4);
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(sp.views);
+    uint32_t* dst = reinterpret_cast<uint32_t*>(s_views);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+  }
+  __syncthreads();
   const int t = threadIdx.x;
   const uint32_t g = blockIdx.x * blockDim.x + t;
   if (g >= sp.n) return;
@@ -207,7 +221,7 @@ __global__ void __launch_bounds__(kPrepThreads, 8) k_preprocess(DevBuffers b) {
   gauss_cov3(get, gc);
   const float smax_g = alpha_skip_bound(gc.opacity);
   for (uint32_t v = 0; v < sp.num_views; ++v) {
-    const ViewInfo& vi = sp.views[v];
+    const ViewInfo& vi = s_views[v];
     ProjOut o;
     const bool ok = project_gaussian(get, gc, vi, sp, deg, true, o);
     const size_t item = (size_t)v * sp.n + g;
@@ -1780,8 +1794,9 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
 // Launchers
 // ---------------------------------------------------------------------------
 void launch_preprocess(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s) {
-  (void)views;
-  k_preprocess<<<(n + kPrepThreads - 1) / kPrepThreads, kPrepThreads, 0, s>>>(b);
+  // the step's cameras in dynamic shared memory (3 KB for 16 views: 8 blocks
+  // of 27 KB stay resident per multiprocessor)
+  k_preprocess<<<(n + kPrepThreads - 1) / kPrepThreads, kPrepThreads, views * sizeof(ViewInfo), s>>>(b);
 }
 
 void launch_scan(const DevBuffers& b, uint32_t n_items, cudaStream_t s) {
