@@ -608,7 +608,8 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
     // this warp's splats of the batch, in order (skipped splats cannot pass
     // the alpha test at any pixel of the warp)
     uint32_t nlist = 0;
-    for (uint32_t base = 0; base < cnt; base += 32) {
+    const bool warp_live = !__all_sync(kFull, done);  // a finished warp lists nothing
+    for (uint32_t base = 0; warp_live && base < cnt; base += 32) {
       const uint32_t j = base + lane;
       const bool in = j < cnt && (s_mask[j] & wbit);
       const uint32_t m = __ballot_sync(kFull, in);
