@@ -1679,15 +1679,22 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   };
   stage(0, 0);
   cp_async_commit();
+  // with culled lists the statistics count the rectangle's tiles instead,
+  // loaded one view ahead as well
+  const bool rect_tiles = stats && sp.tile_cull;
   uint32_t cnt_next = b.counts[g];
+  uint32_t area_next = rect_tiles ? rect_area(b.rects[g]) : 0u;
   for (uint32_t v = 0; v < sp.num_views; ++v) {
     const size_t item = (size_t)v * sp.n + g;
     const int buf = (int)(v & 1u);
     if (v + 1 < sp.num_views) stage(v + 1, buf ^ 1);
     cp_async_commit();
     cp_async_wait1();  // every group but the newest is complete: view v's copy
-    const uint32_t cnt = cnt_next;
-    if (v + 1 < sp.num_views) cnt_next = b.counts[item + sp.n];
+    const uint32_t cnt = cnt_next, area = area_next;
+    if (v + 1 < sp.num_views) {
+      cnt_next = b.counts[item + sp.n];
+      if (rect_tiles) area_next = rect_area(b.rects[item + sp.n]);
+    }
     float4 a0 = make_float4(0.f, 0.f, 0.f, 0.f), a1 = a0, a2 = a0;
     if (cnt > 0u && !ref) {
       a0 = s_is[buf][0][t];
@@ -1700,7 +1707,7 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
       imp.z = imp.z * sp.importance_decay;
       // the statistic counts the tiles of the item's rectangle, also when
       // the intersection lists hold only the tiles its ellipse reaches
-      const uint32_t tiles = sp.tile_cull ? rect_area(b.rects[item]) : cnt;
+      const uint32_t tiles = rect_tiles ? area : cnt;
       if (tiles > 0u) {
         imp.x = imp.x + (float)tiles;
         imp.y = imp.y + 1.0f;
