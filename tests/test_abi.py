@@ -54,6 +54,11 @@ def test_config_size_is_checked_before_touching_the_device(sky):
         assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
         assert b"batch" in L.sky_last_error()
     assert sky.default_config().fwd_batch == 0 and sky.default_config().bwd_batch == 0
+    # culled lists are a switch, off by default (the reference's lists)
+    assert sky.default_config().tile_cull == 0
+    c = sky.default_config(tile_cull=2)
+    assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
+    assert b"tile_cull" in L.sky_last_error()
 
 
 def test_pinhole_camera_matches_reference_projection(sky):
