@@ -150,6 +150,12 @@ typedef struct SkyStatus {
   uint32_t scored_views;      /* views behind the current multi-view scores */
   uint32_t densify_runs;      /* sky_densify calls that changed the scene   */
   uint32_t prune_runs;        /* prunes that removed Gaussians              */
+  uint64_t step_h2d_bytes;    /* host->device bytes the passes copied (step
+                                 parameters), cumulative                    */
+  uint64_t step_d2h_bytes;    /* device->host bytes the passes copied (step
+                                 status: loss, counts), cumulative; images
+                                 and gradients returned by sky_render /
+                                 sky_backward are not included              */
 } SkyStatus;
 
 /* Stages timed by sky_set_profiling / sky_get_stage_times, in order.  The
@@ -262,6 +268,13 @@ typedef struct SkySchedule {
 #define SKY_BUF_GRADS 15       /* 59 gradient planes of the last backward         */
 #define SKY_BUF_GROUPS 16      /* per sort group: begin, end intersection, u32    */
 #define SKY_BUF_DEPTH_RADIUS 18 /* per (view, Gaussian) camera depth, radius, f32 */
+#define SKY_BUF_PAIR_COUNTS 21  /* 6 u64 of the last pass, counted only at profiling
+                                   level 2 (16x16 tiles, default batch depths):
+                                   forward (pixel, splat) pairs evaluated, pairs
+                                   composited, warp list entries (32 pixels
+                                   each); backward pixel pairs evaluated, pairs
+                                   contributing, warp list entries (64 pixels
+                                   each)                                         */
 #define SKY_BUF_STEP_SCALARS 17 /* f32: lr pos, scale, rot, opacity, sh, beta1,
                                    beta2, eps, bias-correction 1/bc1, 1/sqrt(bc2),
                                    SH degree, SH-update flag                     */
@@ -369,7 +382,7 @@ int sky_set_schedule(void* ctx, const SkySchedule* s);
 
 /* ---- headless viewer frame --------------------------------------------------
  * The viewer path of frame(encoder, view) (gaussian-renderer.ts:4111-4123):
- * preprocess.wgsl:116-204 per Gaussian, a global back-to-front depth sort,
+ * preprocess.wgsl:116-215 per Gaussian, a global back-to-front depth sort,
  * and one quad of half-width ceil(3 sqrt(lambda_max)) per splat blended
  * "over" (src-alpha, one-minus-src-alpha; gaussian.wgsl:15-67) into a target
  * cleared to transparent black.  The swapchain texture becomes an f32 RGBA
@@ -401,7 +414,9 @@ int sky_sync(void* ctx);
  * caller can order its own work (or CUDA events) against it.
  * sky_set_profiling(1) resets and starts per-stage timing (profiledTrainStep,
  * gaussian-renderer.ts:3662-3742); sky_get_stage_times returns the summed
- * milliseconds of SKY_NUM_STAGES stages and the number of timed steps.     */
+ * milliseconds of SKY_NUM_STAGES stages and the number of timed steps.
+ * sky_set_profiling(2) also runs the rasterizers' counting variants, which
+ * fill SKY_BUF_PAIR_COUNTS (same results, somewhat slower); 0 stops.      */
 int sky_get_stream(void* ctx, void** stream);
 int sky_set_profiling(void* ctx, int enabled);
 int sky_get_stage_times(void* ctx, double* ms, uint32_t n, uint64_t* steps);
@@ -423,8 +438,12 @@ int sky_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* k
  * until the process exits), so n is limited to SKY_SORT_NOALLOC_MAX_KEYS
  * (larger n returns SKY_ERR_ARG).  The first call on a device looks up that
  * array's address with the device current; make it before any stream
- * capture begins.  All calls share the array: calls whose GPU work overlaps
- * race with each other and must be serialised.                             */
+ * capture begins.  The address is kept for the life of the process, so a
+ * cudaDeviceReset after that first call is not supported (the same holds for
+ * the scratch sky_sort_pairs caches).  All calls share the array: calls whose
+ * GPU work overlaps race with each other and must be serialised.  Like
+ * sky_sort_pairs, the call returns once the sort has finished: it reads the
+ * sort's error word back and waits for `stream`.                          */
 #define SKY_SORT_NOALLOC_MAX_KEYS (1u << 20)
 int sky_sort_pairs_noalloc(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* keys_out,
                            uint32_t* vals_out, uint32_t n, uint32_t key_bits, void* stream);

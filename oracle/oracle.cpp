@@ -202,8 +202,8 @@ void parallel_for(uint32_t n, uint32_t nthreads, Fn fn) {
 }
 
 // ---------------------------------------------------------------------------
-// Projection: training-tiles.wgsl:94-244 (project_gaussians_for_tiling) with
-// the SH colour of training-forward-tiles.wgsl:65-105 / preprocess.wgsl:199-229
+// Projection: training-tiles.wgsl:40-180 (project_gaussians_for_tiling) with
+// the SH colour of training-forward-tiles.wgsl:65-105 / preprocess.wgsl:69-99
 // and the sigmoid of training-forward-tiles.wgsl:188.
 // ---------------------------------------------------------------------------
 template <typename F>
@@ -306,12 +306,12 @@ void project_one(Src&& get, const Cam& cam, const Settings& s, int sh_deg, Rec<F
   mat4_vec<F>(cam.proj, pc, clip);
   F w = clip[3];
   F ndc_x = clip[0] / w, ndc_y = clip[1] / w;
-  // training-tiles.wgsl:131-144
+  // training-tiles.wgsl:67-80
   if (std::fabs(ndc_x) > (F)1.2f || std::fabs(ndc_y) > (F)1.2f || pc[2] <= (F)0.0) return;
   F depth = pc[2];
   if (depth < (F)s.near_plane || depth > (F)s.far_plane) return;
 
-  // :147-162 scale and rotation
+  // :82-98 scale and rotation
   F ls[3];
   for (int k = 0; k < 3; ++k) ls[k] = std::min(std::max(get(3 + k), (F)-10.0), (F)10.0);
   F sig[3] = {ex(ls[0]), ex(ls[1]), ex(ls[2])};
@@ -322,7 +322,7 @@ void project_one(Src&& get, const Cam& cam, const Settings& s, int sh_deg, Rec<F
   F qlen = sq(qq);
   for (int k = 0; k < 4; ++k) q[k] = q[k] / qlen;
   F rx = q[0], ry = q[1], rz = q[2], rw = q[3];
-  // quat_to_mat3_tiling (:94-101), WGSL column-major: R[col][row]
+  // quat_to_mat3_tiling (:30-37), WGSL column-major: R[col][row]
   F R[3][3];
   R[0][0] = (F)1.0 - (F)2.0 * (ry * ry + rz * rz);
   R[0][1] = (F)2.0 * (rx * ry - rw * rz);
@@ -333,7 +333,7 @@ void project_one(Src&& get, const Cam& cam, const Settings& s, int sh_deg, Rec<F
   R[2][0] = (F)2.0 * (rx * rz - rw * ry);
   R[2][1] = (F)2.0 * (ry * rz + rw * rx);
   R[2][2] = (F)1.0 - (F)2.0 * (rx * rx + ry * ry);
-  // C3D = transpose(S * R) * S * R (:165); SR[j][r] = sig[r] * R[j][r];
+  // C3D = transpose(S * R) * S * R (:101); SR[j][r] = sig[r] * R[j][r];
   // A = transpose(SR) * S, A[j][r] = SR[r][j] * sig[j]; C3D = A * R.
   F A[3][3];
   for (int j = 0; j < 3; ++j)
@@ -346,7 +346,7 @@ void project_one(Src&& get, const Cam& cam, const Settings& s, int sh_deg, Rec<F
       acc = acc + A[2][r] * R[j][2];
       C3[j][r] = acc;
     }
-  // J (:170-174), Rwc (:176), T = J * Rwc (:177)
+  // J (:106-110), Rwc (:112), T = J * Rwc (:113)
   F tx = pc[0], ty = pc[1], tz = pc[2];
   F fx = (F)cam.focal[0], fy = (F)cam.focal[1];
   F tz2 = tz * tz;
@@ -359,7 +359,7 @@ void project_one(Src&& get, const Cam& cam, const Settings& s, int sh_deg, Rec<F
     T[j][1] = J11 * v1;
     T[j][2] = J02 * v0 + J12 * v1;
   }
-  // C2D = T * C3D * transpose(T) (:179); B = T * C3D, B[j][r] = sum_k T[k][r] C3[j][k]
+  // C2D = T * C3D * transpose(T) (:115); B = T * C3D, B[j][r] = sum_k T[k][r] C3[j][k]
   F B0[3], B1[3];  // B[j][0], B[j][1]
   for (int j = 0; j < 3; ++j) {
     F a0 = T[0][0] * C3[j][0];
@@ -399,7 +399,7 @@ void project_one(Src&& get, const Cam& cam, const Settings& s, int sh_deg, Rec<F
   o.mean[1] = ((F)0.5 * (ndc_y + (F)1.0)) * H;
   o.radius = radius;
   o.depth = depth;
-  // :226-243 tile rectangle
+  // :161-179 tile rectangle
   F ts = (F)(float)s.tile_size;
   uint32_t TW = (cam.width + s.tile_size - 1) / s.tile_size;
   uint32_t TH = (cam.height + s.tile_size - 1) / s.tile_size;
@@ -431,7 +431,7 @@ uint32_t tiles_w(const Cam& c, const Settings& s) { return (c.width + s.tile_siz
 uint32_t tiles_h(const Cam& c, const Settings& s) { return (c.height + s.tile_size - 1) / s.tile_size; }
 
 // Key of one intersection: (tile << 16) | u32(clamp(depth, 0, 65535)) & 0xFFFF.
-// encode_isect_key (training-tiles.wgsl:192-198) with camera 0 and a tile
+// encode_isect_key (training-tiles.wgsl:193-199) with camera 0 and a tile
 // field wide enough for the view (identical to the 12-bit field when the
 // view has at most 4096 tiles).
 uint32_t isect_key(uint32_t tile, float depth) {
@@ -601,8 +601,8 @@ int orc_project(const float* params, uint64_t stride, uint32_t n, const OrcCam* 
 }
 
 // Host cumsum (gaussian-renderer.ts:1814-1828), emission (training-tiles.wgsl:
-// 265-311), stable sort (radix_sort.wgsl, an LSD radix sort, is stable) and
-// tile offsets with the backward min-fill (training-tiles.wgsl:313-335,
+// 202-247), stable sort (radix_sort.wgsl, an LSD radix sort, is stable) and
+// tile offsets with the backward min-fill (training-tiles.wgsl:250-271,
 // gaussian-renderer.ts:1966-2020).  Arrays of size n_isect must be allocated
 // by the caller (n_isect = sum of counts).
 int orc_tiles(const float* rec12, const uint32_t* counts, const uint32_t* rects, uint32_t n,
@@ -966,7 +966,7 @@ int orc_backward(const float* rec12, uint32_t n, const OrcCam* cam_in, const Orc
 // Exact adjoint of the projection for one view: from the per-Gaussian sums
 // of (dL/dcolour, dL/dlogit, dL/dconic, dL/dmean) to the 59 parameter
 // planes, accumulated (+=) into grads.  Differentiates the forward as
-// implemented (training-tiles.wgsl:126-223, incl. its perspective-free 2D
+// implemented (training-tiles.wgsl:40-180, incl. its perspective-free 2D
 // covariance) with straight-through f16 rounding.  sh_deg: active degree;
 // with_sh == 0 skips the SH planes (steps that do not update them).
 // ---------------------------------------------------------------------------
@@ -1258,7 +1258,7 @@ double orc_loss_f64(const double* params, uint64_t stride, uint32_t n, const Orc
 }
 
 // ---------------------------------------------------------------------------
-// Viewer frame (gaussian-renderer.ts:4111-4123): preprocess.wgsl:116-204 per
+// Viewer frame (gaussian-renderer.ts:4111-4123): preprocess.wgsl:116-215 per
 // Gaussian, a stable ascending sort of float_to_ordered_uint(-z_camera)
 // (:94-98; the reference's atomic compaction order is replaced by index
 // order), then one quad per splat drawn in that order (gaussian.wgsl:15-67)

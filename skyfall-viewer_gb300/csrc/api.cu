@@ -56,16 +56,21 @@ int fail(int code, const char* fmt, ...) {
 
 // Host-side fault injection for tests of the error paths: SKY_FAULT=alloc:N
 // makes the N-th device allocation (1-based, process wide) fail with
-// SKY_ERR_INJECTED; SKY_FAULT=launch:N makes the N-th step fail before it
-// launches anything.
+// SKY_ERR_INJECTED; SKY_FAULT=launch:N makes the N-th pass (step, forward,
+// backward or render) fail before it launches anything; SKY_FAULT=lookback:N
+// makes the N-th radix sort of a pass (item or intersection sort) or of
+// sky_sort_pairs run its bounded look-back waits out (tile 0 withholds its
+// word, 64 polls; see sort.cu), so that the call reports SKY_ERR_TIMEOUT.
+// Read once, when the first counted event happens.
 struct FaultPlan {
-  long alloc_at = -1, launch_at = -1;
-  long allocs = 0, launches = 0;
+  long alloc_at = -1, launch_at = -1, lookback_at = -1;
+  long allocs = 0, launches = 0, sorts = 0;
   FaultPlan() {
     const char* f = getenv("SKY_FAULT");
     if (!f) return;
     if (!strncmp(f, "alloc:", 6)) alloc_at = atol(f + 6);
     if (!strncmp(f, "launch:", 7)) launch_at = atol(f + 7);
+    if (!strncmp(f, "lookback:", 9)) lookback_at = atol(f + 9);
   }
 };
 std::mutex g_fault_mu;
@@ -83,6 +88,20 @@ bool inject_launch() {
   FaultPlan& p = faults();
   return p.launch_at > 0 && ++p.launches == p.launch_at;
 }
+
+}  // namespace
+
+bool sky::fault_lookback_next(cudaStream_t stream) {
+  std::lock_guard<std::mutex> l(g_fault_mu);
+  FaultPlan& p = faults();
+  if (p.lookback_at <= 0) return false;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone)
+    return false;
+  return ++p.sorts == p.lookback_at;
+}
+
+namespace {
 
 uint64_t splitmix64(uint64_t& s) {
   uint64_t z = (s += 0x9E3779B97F4A7C15ull);
@@ -116,6 +135,7 @@ struct Shape {
   uint32_t key_bits[kMaxGroups] = {};
   uint32_t fwd_batch = 0, bwd_batch = 0;  // splat-batch depths (kernel variants)
   bool with_loss = false, ssim = false, ref = false, prof = false;
+  bool count = false;  // pair-counting raster variants (profiling level 2)
   bool same(const Shape& o) const { return memcmp(this, &o, sizeof(Shape)) == 0; }
 };
 
@@ -163,8 +183,13 @@ struct Context {
   bool fwd_ready = false;
   uint32_t error_flags = 0;
   uint64_t launches = 0;
-  // per-stage profiling (CUDA events on the context's stream)
+  // per-stage profiling (CUDA events on the context's stream); level 2 also
+  // runs the pair-counting raster variants
   bool profiling = false;
+  bool count_pairs = false;
+  // host <-> device bytes copied by the passes (step parameters in, status
+  // out), cumulative; a captured graph's copies are counted per replay
+  uint64_t step_h2d = 0, step_d2h = 0, graph_h2d = 0, graph_d2h = 0;
   cudaEvent_t ev[SKY_NUM_STAGES + 1] = {};
   double stage_ms[SKY_NUM_STAGES] = {};
   uint64_t prof_steps = 0;
@@ -306,7 +331,8 @@ double position_lr(const SkyConfig& cfg, uint64_t iteration) {
 // Enqueues the pass on the context's stream.  With sizing_sync (direct
 // passes only) the intersection count is read back after the scan and the
 // buffers grown before emission, as the reference does with its host cumsum.
-int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
+int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches, uint64_t& h2d,
+            uint64_t& d2h) {
   cudaStream_t s = c->stream;
   DevBuffers b = make_buffers(c);
   const bool prof = sh.prof;
@@ -318,6 +344,8 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
   };
   const uint64_t items = (uint64_t)sh.nv * sh.n;
   launches = 0;
+  h2d = sizeof(StepParams);
+  d2h = 0;
   CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
   CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
   DevStatus* dst = (DevStatus*)c->d_st.p;
@@ -333,7 +361,7 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
       // bounds = {item_begin, item_end} of the group, in device memory
       SortSegment seg{&d_sp->groups[g].item_begin, 0};
       CK(sort_pairs_launch(b.ikeys, nullptr, (uint32_t*)c->ikeys_sorted.p, b.perm, seg,
-                           (uint32_t)items, 16, c->isort, &dst->error, s));
+                           (uint32_t)items, 16, c->isort, &dst->error, s, 0, true));
       launches += 4;
     }
   }
@@ -341,12 +369,16 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
   launch_group_bounds(b, s);
   launches += 5;
   if (sizing_sync) {
+    d2h += sizeof(DevStatus);
     CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    if (c->h_st->total_isect > c->icap) {
+    // (after an error the later kernels of the step do nothing, and the
+    // count is not to be trusted: no growth)
+    if (c->h_st->error == 0u && c->h_st->total_isect > c->icap) {
       TRY(ensure_isect(c, c->h_st->total_isect));
       b = make_buffers(c);
       c->h_sp->icap = c->icap;
+      h2d += sizeof(StepParams);
       CK(cudaMemcpyAsync(c->d_sp.p, c->h_sp, sizeof(StepParams), cudaMemcpyHostToDevice, s));
       CK(cudaMemsetAsync(c->d_st.p, 0, sizeof(DevStatus), s));
       launch_group_bounds(b, s);
@@ -361,19 +393,20 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
     // the tile field (digits 2 and 3) alone gives the full key order
     SortSegment seg{&dst->group_bounds[g][0], 0};
     CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap, sh.key_bits[g],
-                         c->sort, &dst->error, s, 2));
+                         c->sort, &dst->error, s, 2, true));
     launches += 2 + (sh.key_bits[g] + 7) / 8 - 2;
   }
   TRY(mark(4));
   launch_ranges(b, c->icap, s);
   TRY(mark(5));
-  launch_forward(b, sh.max_tiles, c->cfg.tile_size, sh.fwd_batch, sh.ssim, sh.nv, sh.max_view_px, s);
+  launch_forward(b, sh.max_tiles, c->cfg.tile_size, sh.fwd_batch, sh.ssim, sh.nv, sh.max_view_px,
+                 sh.count, s);
   if (sh.with_loss) launch_loss_final(b, s);
   launches += 4 + (sh.with_loss ? 1 : 0) + (sh.ssim ? 1 : 0);
   TRY(mark(6));
   if (sh.mode >= kBackward) {
     if (sh.ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
-    launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.bwd_batch, sh.ref, s);
+    launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.bwd_batch, sh.ref, sh.count, s);
     TRY(mark(7));
     if (!sh.ref) {
       launch_item_sums(b, items, s);
@@ -386,6 +419,7 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches) {
   }
   TRY(mark(8));
   CK(cudaGetLastError());
+  d2h += sizeof(DevStatus);
   CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
   return SKY_OK;
 }
@@ -559,21 +593,22 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   sh.ssim = with_loss && cfg.w_ssim > 0.0f;
   sh.ref = ref;
   sh.prof = c->profiling;
+  sh.count = c->count_pairs;
   sh.fwd_batch = cfg.fwd_batch;
   sh.bwd_batch = cfg.bwd_batch;
   cudaStream_t s = c->stream;
-  uint64_t launches = 0;
+  uint64_t launches = 0, h2d = 0, d2h = 0;
   for (int attempt = 0;; ++attempt) {
     sh.icap = c->icap;
     sp.icap = c->icap;
     if (!graph) {
-      TRY(enqueue(c, sh, true, launches));
+      TRY(enqueue(c, sh, true, launches, h2d, d2h));
     } else {
       if (!c->gvalid || !c->gshape.same(sh)) {
         drop_graph(c);
         CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-        uint64_t l = 0;
-        int rc = enqueue(c, sh, false, l);
+        uint64_t l = 0, gi = 0, go = 0;
+        int rc = enqueue(c, sh, false, l, gi, go);
         cudaGraph_t g = nullptr;
         cudaError_t e = cudaStreamEndCapture(s, &g);
         if (rc != SKY_OK) {
@@ -587,14 +622,20 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
         c->gshape = sh;
         c->gvalid = true;
         c->graph_launches = l;
+        c->graph_h2d = gi;
+        c->graph_d2h = go;
         c->graph_captures += 1;
       }
       CK(cudaGraphLaunch(c->gexec, s));
       launches = c->graph_launches;
+      h2d = c->graph_h2d;
+      d2h = c->graph_d2h;
       c->graph_replays += 1;
     }
     CK(cudaStreamSynchronize(s));
     c->launches += launches;
+    c->step_h2d += h2d;
+    c->step_d2h += d2h;
     if (graph && (c->h_st->error & SKY_DEVERR_CAPACITY) && attempt < 3) {
       // the failed replay changed no parameter: grow, re-capture, run again
       TRY(ensure_isect(c, c->h_st->total_isect));
@@ -614,6 +655,10 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   c->error_flags |= c->h_st->error;
   if (c->h_st->error & SKY_DEVERR_SORT_TIMEOUT)
     return fail(SKY_ERR_TIMEOUT, "radix sort look-back wait gave up");
+  if (c->h_st->error & SKY_DEVERR_LISTS)
+    return fail(SKY_ERR_STATE,
+                "intersection lists inconsistent: key emission disagreed with the preprocess's "
+                "tile counts, or the tile ranges met unsorted keys");
   if (c->h_st->error & SKY_DEVERR_CAPACITY)
     return fail(SKY_ERR_CAPACITY, "intersection capacity exceeded");
   c->last_views.assign(cams, cams + nv);
@@ -1595,6 +1640,8 @@ int sky_get_status(void* p, SkyStatus* st) {
   st->scored_views = c->scores_views;
   st->densify_runs = c->densify_runs;
   st->prune_runs = c->prune_runs;
+  st->step_h2d_bytes = c->step_h2d;
+  st->step_d2h_bytes = c->step_d2h;
   return SKY_OK;
 }
 
@@ -1639,6 +1686,11 @@ int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* siz
       if (dst && bytes >= sizeof(v)) memcpy(dst, v, sizeof(v));
       return SKY_OK;
     }
+    case SKY_BUF_PAIR_COUNTS: {
+      if (size_out) *size_out = sizeof(c->h_st->pairs);
+      if (dst && bytes >= sizeof(c->h_st->pairs)) memcpy(dst, c->h_st->pairs, sizeof(c->h_st->pairs));
+      return SKY_OK;
+    }
     case SKY_BUF_GROUPS: {
       if (size_out) *size_out = (uint64_t)c->last_groups * 8;
       if (dst && bytes >= (uint64_t)c->last_groups * 8)
@@ -1676,9 +1728,11 @@ int sky_get_stream(void* p, void** stream) {
 int sky_set_profiling(void* p, int enabled) {
   Context* c = as_ctx(p);
   if (!c) return fail(SKY_ERR_ARG, "null context");
+  if (enabled < 0 || enabled > 2) return fail(SKY_ERR_ARG, "profiling level %d not 0, 1 or 2", enabled);
   if (enabled && !c->ev[0])
     for (int k = 0; k <= SKY_NUM_STAGES; ++k) CK(cudaEventCreate(&c->ev[k]));
   c->profiling = enabled != 0;
+  c->count_pairs = enabled == 2;
   for (int k = 0; k < SKY_NUM_STAGES; ++k) c->stage_ms[k] = 0.0;
   c->prof_steps = 0;
   return SKY_OK;
@@ -1732,7 +1786,8 @@ int sky_sort_pairs(const uint32_t* keys_in, const uint32_t* vals_in, uint32_t* k
   SortScratch scr = sort_scratch_carve(sc.mem, sc.max_n);
   CK(cudaMemsetAsync(sc.err, 0, 4, s));
   SortSegment seg{nullptr, n};
-  CK(sort_pairs_launch(keys_in, vals_in, keys_out, vals_out, seg, n, key_bits, scr, sc.err, s));
+  CK(sort_pairs_launch(keys_in, vals_in, keys_out, vals_out, seg, n, key_bits, scr, sc.err, s, 0,
+                       true));
   uint32_t err = 0;
   CK(cudaMemcpyAsync(&err, sc.err, 4, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

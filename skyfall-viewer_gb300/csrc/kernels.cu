@@ -41,7 +41,7 @@ SKY_DEV bool capacity_failed(const DevStatus* st) {
 SKY_DEV float alpha_skip_bound(float opacity) { return __logf(255.0f * opacity) + 1e-3f; }
 
 // The depth field of an intersection key: u32(clamp(depth, 0, 65535)) & 0xFFFF
-// (encode_isect_key, training-tiles.wgsl:192-198).
+// (encode_isect_key, training-tiles.wgsl:193-199).
 SKY_DEV uint32_t depth_key(float depth) {
   return wgsl_u32(clampf_(depth, 0.0f, 65535.0f)) & 0xFFFFu;
 }
@@ -98,11 +98,20 @@ SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float 
 // within 2.5e-3 U of the exact one; V within 1e-5 V.  The margins (1 % plus
 // 0.05 px) cover that with room, so a pixel column outside [mx + ul, mx + ur]
 // holds no pixel of the band that can pass the pre-filter; a column kept in
-// excess only costs time.
+// excess only costs time.  A band that lies wholly beyond E's top or bottom
+// row but within v_margin of it (w0 > w1) can only hold pixels that pass
+// through that rounding, within 1e-5 V of the extreme row, so it gets the
+// extent of that row (the tip -b v / a at v = +-V, plus the margins).
 SKY_DEV bool band_extent(const EllipseRows& r, float v0, float v1, float& ul, float& ur) {
   if (v1 < -r.v_margin || v0 > r.v_margin) return false;
   const float w0 = fmaxf(v0, -r.V), w1 = fminf(v1, r.V);
-  const float vr = fminf(fmaxf(r.v_right, w0), w1), vl = fminf(fmaxf(-r.v_right, w0), w1);
+  float vr, vl;
+  if (w0 > w1) {
+    vr = vl = v0 > 0.0f ? r.V : -r.V;
+  } else {
+    vr = fminf(fmaxf(r.v_right, w0), w1);
+    vl = fminf(fmaxf(-r.v_right, w0), w1);
+  }
   const float dr = fmaxf(r.two_a_l - r.det * vr * vr, 0.0f);
   const float dl = fmaxf(r.two_a_l - r.det * vl * vl, 0.0f);
   ur = (-r.b * vr + sqrtf(dr)) / r.a + r.u_margin;
@@ -266,8 +275,13 @@ SKY_DEV uint32_t scan_count(const DevBuffers& b, uint32_t i) {
   return c < 0xFFFFu ? c : b.counts[b.perm[i]];
 }
 
+// A scan of a step (b.status set) after a sort that gave up does nothing:
+// the permutation may hold stale words, which must not be used as indices.
+SKY_DEV bool scan_skipped(const DevBuffers& b) { return b.status && capacity_failed(b.status); }
+
 __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevBuffers b, uint32_t n_items) {
   __shared__ uint32_t s_warp[kScanThreads / 32];
+  if (scan_skipped(b)) return;
   const uint32_t base = blockIdx.x * kScanTile;
   uint32_t sum = 0;
   for (int k = 0; k < kScanItems; ++k) {
@@ -281,6 +295,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_reduce(DevBuffers b, uint
 
 __global__ void __launch_bounds__(1024) k_scan_blocks(DevBuffers b, uint32_t nblocks) {
   __shared__ uint32_t s_warp[32];
+  if (scan_skipped(b)) return;
   uint32_t carry = 0;
   for (uint32_t base = 0; base < nblocks; base += 1024) {
     uint32_t i = base + threadIdx.x;
@@ -294,6 +309,7 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(DevBuffers b, uint32_t nbl
 
 __global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint32_t n_items) {
   __shared__ uint32_t s_warp[kScanThreads / 32];
+  if (scan_skipped(b)) return;
   const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
   uint32_t v[kScanItems];
   uint32_t sum = 0;
@@ -317,18 +333,21 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint3
 }
 
 // Group bounds of the sort segments and the capacity check.
+// After an earlier error (the item sort gave up, so the scan was skipped)
+// the step has no intersections: every group is empty.
 __global__ void k_group_bounds(DevBuffers b) {
   const StepParams& sp = *b.sp;
   const uint32_t items = sp.num_views * sp.n;
-  const uint32_t total = items ? b.cumsum[items - 1] : 0u;
+  const bool failed = capacity_failed(b.status);
+  const uint32_t total = (items && !failed) ? b.cumsum[items - 1] : 0u;
   if (threadIdx.x == 0) {
     b.status->total_isect = total;
     if (total > sp.icap) atomicOr(&b.status->error, SKY_DEVERR_CAPACITY);
   }
   for (uint32_t g = threadIdx.x; g < sp.num_groups; g += blockDim.x) {
     const GroupInfo& gi = sp.groups[g];
-    uint32_t lo = gi.item_begin ? b.cumsum[gi.item_begin - 1] : 0u;
-    uint32_t hi = gi.item_end ? b.cumsum[gi.item_end - 1] : 0u;
+    uint32_t lo = (gi.item_begin && !failed) ? b.cumsum[gi.item_begin - 1] : 0u;
+    uint32_t hi = (gi.item_end && !failed) ? b.cumsum[gi.item_end - 1] : 0u;
     b.status->group_bounds[g][0] = min(lo, sp.icap);
     b.status->group_bounds[g][1] = min(hi, sp.icap);
   }
@@ -336,7 +355,7 @@ __global__ void k_group_bounds(DevBuffers b) {
 
 // ---------------------------------------------------------------------------
 // Key emission: (key_tile << 16) | depth16 in row-major tile order per item
-// -- emit_intersections (training-tiles.wgsl:265-311) with a per-group tile
+// -- emit_intersections (training-tiles.wgsl:202-247) with a per-group tile
 // field.  Items are emitted in perm order -- per sort group, by depth16, ties
 // in (view, Gaussian) order -- not in (view, Gaussian) order.  A tile belongs
 // to one view, so a stable sort of these keys on the tile field alone yields
@@ -348,6 +367,7 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t v = blockIdx.y;
   if (g >= sp.n || v >= sp.num_views) return;
+  if (capacity_failed(b.status)) return;  // perm / cumsum are not to be trusted
   const uint32_t pos = v * sp.n + g;  // position in emission (perm) order
   // items of one sort group's views interleave: the view is the item's own;
   // the sorted item key carries its depth field
@@ -392,14 +412,14 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const float cc = b.records[(size_t)item * 3 + 1].x, smax = b.records[(size_t)item * 3 + 2].y;
   EllipseRows e;
   if (!ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
-    atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);  // counted differently: corrupt lists
+    atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
     return;
   }
   for (uint32_t ty = y0; ty < y1; ++ty) {
     uint32_t lo;
     const uint32_t len = row_span(e, ty, x0, x1, sp.tile_size, lo);
     if (len > end - cur) {
-      atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);
+      atomicOr(&b.status->error, SKY_DEVERR_LISTS);
       return;
     }
     for (uint32_t tx = lo; tx < lo + len; ++tx) {
@@ -409,13 +429,13 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
       ++cur;
     }
   }
-  if (cur != end) atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);
+  if (cur != end) atomicOr(&b.status->error, SKY_DEVERR_LISTS);
 }
 
 // ---------------------------------------------------------------------------
 // Tile ranges: offsets[t] = first sorted intersection of tile t, empty tiles
 // take the start of the next non-empty one (build_tile_offsets +
-// host backward min-fill, training-tiles.wgsl:313-335 and
+// host backward min-fill, training-tiles.wgsl:250-271 and
 // gaussian-renderer.ts:1966-2020).  Also resolves the item of every sorted
 // intersection.
 // ---------------------------------------------------------------------------
@@ -433,7 +453,7 @@ __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
     const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
     const uint32_t t = gi.tile_begin + (b.keys_sorted[i] >> 16);
     if (t >= gi.tile_end || (i > gb && gi.tile_begin + (b.keys_sorted[i - 1] >> 16) > t)) {
-      atomicOr(&b.status->error, SKY_DEVERR_SORT_TIMEOUT);  // unsorted or corrupt keys
+      atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // unsorted or corrupt keys
       return;
     }
     if (i == gb) {
@@ -561,7 +581,27 @@ SKY_DEV void stage_record(float4* dst, const float4& q0, const float4& q1, const
 // (+0 or positive) + (b dx) dy, and +0 + -0 = +0).
 SKY_DEV bool outside_smax(float s, float smax) { return __float_as_uint(s) > __float_as_uint(smax); }
 
-template <int TS, int FB>
+// Warp sums of the counting variants' per-lane tallies of evaluated and
+// contributing pairs, and lane 0's count of the warp's list entries, added
+// to the step's status counters pairs[base..base+2].
+SKY_DEV void add_pair_counts(const DevBuffers& b, int base, uint32_t eval, uint32_t contrib,
+                             uint32_t entries) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    eval += __shfl_xor_sync(kFull, eval, o);
+    contrib += __shfl_xor_sync(kFull, contrib, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(&b.status->pairs[base + 0], (unsigned long long)eval);
+    atomicAdd(&b.status->pairs[base + 1], (unsigned long long)contrib);
+    atomicAdd(&b.status->pairs[base + 2], (unsigned long long)entries);
+  }
+}
+
+// CNT: the counting variant (profiling level 2) also tallies the pairs it
+// evaluates and composites and the list entries its warps walk; the
+// arithmetic and every result are those of the plain variant.
+template <int TS, int FB, bool CNT = false>
 __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   static_assert(FB <= 256, "list entries are bytes");
   constexpr int NT = TS * TS;
@@ -593,6 +633,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
   bool done = !inside;
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
+  uint32_t n_eval = 0, n_contrib = 0, n_entries = 0;  // counting variant only
   for (uint32_t bs = start; bs < end; bs += FB) {
     const uint32_t cnt = min((uint32_t)FB, end - bs);
     __syncthreads();
@@ -617,6 +658,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
       nlist += __popc(m);
     }
     __syncwarp();
+    if constexpr (CNT) n_entries += nlist;
     if (!done) {
       for (uint32_t li = 0; li < nlist; ++li) {
         const uint32_t j = s_list[warp][li];
@@ -628,12 +670,14 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
         const float s2 = (r1.x * dy) * dy;
         float so2 = s1 + s2;
         so2 = so2 + (r0.w * dx) * dy;
+        if constexpr (CNT) ++n_eval;
         if (outside_smax(so2, r2.y)) continue;
         // emitted records have finite means and conics, so 0 <= s <= s_max
         const float G = sky_expf_inrange(-so2);
         const float al = r1.y * G;
         const float a = fmin_(al, MAX_ALPHA);
         if (a < MIN_ALPHA) continue;
+        if constexpr (CNT) ++n_contrib;
         const float om = 1.0f - A;
         const float ca = a * om;
         C0 = C0 + r1.z * ca;
@@ -650,6 +694,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
     }
     if (__syncthreads_and(done)) break;
   }
+  if constexpr (CNT) add_pair_counts(b, 0, n_eval, n_contrib, n_entries);
   double lpx = 0.0;
   if (inside) {
     const size_t p = (size_t)vi.pixel_base + (size_t)y * vi.width + x;
@@ -1066,7 +1111,7 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
 
 // BB: the splat-batch depth (32, 64 or 128 staged splats); the per-splat sums
 // do not depend on it.
-template <int BB>
+template <int BB, bool CNT = false>
 __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   static_assert(BB <= 256, "list entries are bytes");
   constexpr int TS = 16, NT = 128, NW = 4, kBatch = BB;
@@ -1118,6 +1163,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   const int slot = scatter9_slot(lane);
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
+  uint32_t n_eval = 0, n_contrib = 0, n_entries = 0;  // counting variant only
   // intersections no pixel reaches get zero partials
   for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
     float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
@@ -1156,8 +1202,17 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float dx = pix[0].px - q0.x;
       const float s1 = (q0.z * dx) * dx, bdx = q0.w * dx;
       bool contrib = false;
-      if (i <= pix[0].hi) contrib = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, val);
-      if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val) || contrib;
+      if constexpr (CNT) {
+        ++n_entries;
+        bool c0 = false, c1 = false;
+        if (i <= pix[0].hi) { ++n_eval; c0 = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, val); }
+        if (i <= pix[1].hi) { ++n_eval; c1 = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val); }
+        n_contrib += (uint32_t)c0 + (uint32_t)c1;
+        contrib = c0 || c1;
+      } else {
+        if (i <= pix[0].hi) contrib = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, val);
+        if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val) || contrib;
+      }
       const uint32_t who = __ballot_sync(kFull, contrib);
       if (who == 0u) {
         if (slot < 9) s_part[warp][j][slot] = 0.0f;
@@ -1195,6 +1250,8 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
     }
   }
+  // (every lane walks the warp's list: lane 0's n_entries is the warp's)
+  if constexpr (CNT) add_pair_counts(b, 3, n_eval, n_contrib, n_entries);
 }
 
 // ---------------------------------------------------------------------------
@@ -1357,7 +1414,7 @@ __global__ void __launch_bounds__(TS* TS) k_backward_ref(DevBuffers b) {
 // of the step: sum the Gaussian's per-intersection partials (contiguous in
 // emission order, summed in order), then back-propagate dL/d(colour, logit,
 // conic, mean2d) through the projection as implemented (training-tiles.wgsl:
-// 126-223) to position, log sigma, quaternion, opacity logit and SH.  The
+// 40-180) to position, log sigma, quaternion, opacity logit and SH.  The
 // per-view gradients are added in view order.  Then adam.wgsl:18-38 per
 // plane with the group's learning rate.
 // ---------------------------------------------------------------------------
@@ -1833,7 +1890,12 @@ void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s) {
 }
 
 template <int TS>
-void launch_forward_ts(const DevBuffers& b, uint32_t max_tiles, uint32_t fb, cudaStream_t s) {
+void launch_forward_ts(const DevBuffers& b, uint32_t max_tiles, uint32_t fb, bool count,
+                       cudaStream_t s) {
+  if (TS == 16 && count && (fb == 0 || fb == (uint32_t)kFwdBatch)) {
+    k_forward<TS, kFwdBatch, true><<<max_tiles, TS * TS, 0, s>>>(b);
+    return;
+  }
   switch (fb) {
     case 64: k_forward<TS, 64><<<max_tiles, TS * TS, 0, s>>>(b); break;
     case 128: k_forward<TS, 128><<<max_tiles, TS * TS, 0, s>>>(b); break;
@@ -1842,12 +1904,12 @@ void launch_forward_ts(const DevBuffers& b, uint32_t max_tiles, uint32_t fb, cud
 }
 
 void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t fb, bool ssim,
-                    uint32_t views, uint32_t max_view_pixels, cudaStream_t s) {
+                    uint32_t views, uint32_t max_view_pixels, bool count, cudaStream_t s) {
   if (max_tiles == 0) return;
   switch (ts) {
-    case 8: launch_forward_ts<8>(b, max_tiles, fb, s); break;
-    case 32: launch_forward_ts<32>(b, max_tiles, fb, s); break;
-    default: launch_forward_ts<16>(b, max_tiles, fb, s); break;
+    case 8: launch_forward_ts<8>(b, max_tiles, fb, false, s); break;
+    case 32: launch_forward_ts<32>(b, max_tiles, fb, false, s); break;
+    default: launch_forward_ts<16>(b, max_tiles, fb, count, s); break;
   }
   if (ssim) {
     dim3 grid((max_view_pixels + 255) / 256, views);
@@ -1858,13 +1920,17 @@ void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32
 void launch_loss_final(const DevBuffers& b, cudaStream_t s) { k_loss_final<<<1, 1024, 0, s>>>(b); }
 
 void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t bb, bool ref,
-                     cudaStream_t s) {
+                     bool count, cudaStream_t s) {
   if (max_tiles == 0) return;
   if (!ref) {
     switch (ts) {
       case 8: k_backward_exact<8><<<max_tiles, 64, 0, s>>>(b); break;
       case 32: k_backward_exact<32><<<max_tiles, 1024, 0, s>>>(b); break;
       default:
+        if (count && (bb == 0 || bb == kBwdBatch16)) {
+          k_backward_exact2<kBwdBatch16, true><<<max_tiles, 128, 0, s>>>(b);
+          break;
+        }
         switch (bb) {
           case 32: k_backward_exact2<32><<<max_tiles, 128, 0, s>>>(b); break;
           case 64: k_backward_exact2<64><<<max_tiles, 128, 0, s>>>(b); break;

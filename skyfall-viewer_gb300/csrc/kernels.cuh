@@ -16,11 +16,13 @@ void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s);
 // batch (64, 128 or 256), the 16x16-tile exact backward bb (32, 64 or 128);
 // other values select the defaults.  Results do not depend on them.
 constexpr uint32_t kBwdBatch16 = 128;  // default backward depth for 16x16 tiles
+// count: the pair-counting variants (16x16 tiles at the default depths
+// only; other shapes launch the plain kernels and count nothing).
 void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t fb, bool ssim,
-                    uint32_t views, uint32_t max_view_pixels, cudaStream_t s);
+                    uint32_t views, uint32_t max_view_pixels, bool count, cudaStream_t s);
 void launch_loss_final(const DevBuffers& b, cudaStream_t s);
 void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t bb, bool ref,
-                     cudaStream_t s);
+                     bool count, cudaStream_t s);
 void launch_geom_adam(const DevBuffers& b, uint32_t n, cudaStream_t s);
 // Exact mode, before launch_geom_adam: per-item sums of the partials.
 void launch_item_sums(const DevBuffers& b, uint64_t items, cudaStream_t s);

@@ -1,6 +1,6 @@
 // Projection of one Gaussian into one view, shared by the preprocess kernel
 // and the geometry adjoint.  Follows project_gaussians_for_tiling
-// (src/shaders/training-tiles.wgsl:94-244) operation for operation in the
+// (src/shaders/training-tiles.wgsl:40-180) operation for operation in the
 // order fixed by sky_math.cuh, plus the per-Gaussian opacity and SH colour
 // the reference evaluates per pixel (training-forward-tiles.wgsl:184-190).
 #pragma once
@@ -32,7 +32,8 @@ struct GaussCov3 {
 };
 
 // Quaternion (planes 6..9) normalised and turned into the rotation matrix,
-// R[a][c] = row a, column c of the rotation (training-tiles.wgsl:139-152).
+// R[a][c] = row a, column c of the rotation (quat_to_mat3_tiling,
+// training-tiles.wgsl:30-37, of the quaternion read at :97-98).
 template <typename Get>
 SKY_DEV void gauss_rotation(Get get, float R[3][3], float qn[4], float& ql) {
   float q0 = get(6), q1 = get(7), q2 = get(8), q3 = get(9);

@@ -64,6 +64,11 @@ struct DevStatus {
   uint32_t group_bounds[kMaxGroups][2];  // [begin, end) clamped to capacity
   double loss;
   double pad2;
+  // Work counters of the rasterizers, filled only by their counting variants
+  // (profiling level 2): forward (pixel, splat) pairs evaluated, pairs
+  // composited, warp list entries; backward pixel pairs evaluated, pairs
+  // contributing, warp list entries (each entry covers 64 pixels).
+  unsigned long long pairs[6];
 };
 
 // Device buffers of a context (all owned by the host runtime).

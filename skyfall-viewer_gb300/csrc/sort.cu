@@ -157,7 +157,8 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
            uint32_t* vals_dst_out, uint32_t* keys_tmp, uint32_t* vals_tmp, SortSegment seg,
            int pass, int passes, int digit_lo, const uint32_t* __restrict__ trivial, uint32_t key_bits,
            const uint32_t* __restrict__ hist, uint32_t* __restrict__ tile_counter,
-           uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err) {
+           uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err,
+           uint32_t spin_limit, uint32_t withhold_tile0) {
   __shared__ uint32_t s_keys[kSortTile];
   __shared__ uint32_t s_vals[kSortTile];
   __shared__ uint32_t s_warp_hist[kWarps][kRadix];
@@ -249,7 +250,10 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
     run += c;
   }
   uint32_t* lb = lookback + ((uint64_t)pass * max_tiles) * kRadix;
-  st_relaxed(&lb[(uint64_t)tile * kRadix + d], (tile == 0 ? kFlagPrefix : kFlagAgg) | run);
+  // (host fault injection only: tile 0 keeps its word back, so tile 1's
+  // bounded wait runs out)
+  if (tile != 0 || !withhold_tile0)
+    st_relaxed(&lb[(uint64_t)tile * kRadix + d], (tile == 0 ? kFlagPrefix : kFlagAgg) | run);
 
   // Exclusive scan of tile counts over digits.
   uint32_t x = run;
@@ -269,7 +273,7 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
       uint32_t v = ld_relaxed(&lb[(uint64_t)j * kRadix + d]);
       uint32_t flag = v & ~kValueMask;
       if (flag == 0u) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicOr(err, SKY_DEVERR_SORT_TIMEOUT);
           break;
         }
@@ -362,7 +366,8 @@ SortScratch sort_scratch_carve(void* base, uint32_t max_n) {
 cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
-                              uint32_t* err, cudaStream_t stream, int digit_lo) {
+                              uint32_t* err, cudaStream_t stream, int digit_lo,
+                              bool fault_point) {
   if (key_bits == 0) key_bits = 1;
   if (key_bits > 32) key_bits = 32;
   const int passes = (int)((key_bits + 7) / 8);
@@ -378,12 +383,20 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                                                          sc.hist, sc.lookback, sc.max_tiles);
   uint32_t* trivial = sc.tile_counter + 8;  // cleared with the tile tickets above
   k_sort_scan<<<passes, kRadix, 0, stream>>>(sc.hist, seg, trivial, digit_lo);
+  // Host fault injection (SKY_FAULT=lookback:N): in the N-th fault-point sort
+  // of the process, tile 0 of every digit pass withholds its look-back word
+  // and the waits give up after 64 polls -- the timeout path, without a
+  // hang.  Never taken while a graph is being captured (the fault would be
+  // replayed).
+  const bool inject = fault_point && fault_lookback_next(stream);
+  const uint32_t spin_limit = inject ? 64u : kSpinLimit;
   for (int p = digit_lo; p < passes; ++p)
     k_onesweep<<<std::min<uint32_t>(tiles, (uint32_t)sm_count() * 4), kSortThreads, 0,
                  stream>>>(keys_in, vals_in, keys_out, vals_out,
                                                     sc.keys_tmp, sc.vals_tmp, seg, p, passes,
                                                     digit_lo, trivial, key_bits, sc.hist,
-                                                    sc.tile_counter, sc.lookback, sc.max_tiles, err);
+                                                    sc.tile_counter, sc.lookback, sc.max_tiles, err,
+                                                    spin_limit, inject ? 1u : 0u);
   return cudaGetLastError();
 }
 

@@ -26,6 +26,10 @@ constexpr int kMaxPasses = 4;
 // Device error bits (status word 0).
 constexpr uint32_t SKY_DEVERR_CAPACITY = 1u;
 constexpr uint32_t SKY_DEVERR_SORT_TIMEOUT = 2u;
+// The intersection lists disagree with themselves: key emission wrote a
+// different number of tiles than the preprocess counted for an item, or the
+// tile ranges met sorted keys out of order.  Later kernels of the step skip.
+constexpr uint32_t SKY_DEVERR_LISTS = 4u;
 
 struct SortScratch {
   uint32_t* hist;          // kMaxPasses * 256 digit counts, then exclusive offsets
@@ -50,10 +54,19 @@ struct SortSegment {
 // digit_lo: 8-bit digits below it are not sorted on -- for keys whose input
 // order is already ascending in those bits among equal higher bits, the
 // result is the full sort.
+// fault_point: the sort counts for SKY_FAULT=lookback:N (host fault
+// injection, used by tests); only callers whose later kernels check the
+// error word before indexing with the sort's output pass true.
 cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
-                              uint32_t* err, cudaStream_t stream, int digit_lo = 0);
+                              uint32_t* err, cudaStream_t stream, int digit_lo = 0,
+                              bool fault_point = false);
+
+// Host fault injection (SKY_FAULT=lookback:N, api.cu): true for the N-th
+// fault-point sort launched outside graph capture in the process.  Without
+// that setting it returns false and makes no CUDA call.
+bool fault_lookback_next(cudaStream_t stream);
 
 // Multiprocessors of the current device (cached per device).
 int sm_count();

@@ -17,11 +17,15 @@
 //    rejected with SKY_ERR_ARG (use sky_sort_pairs for those);
 //  * the first call on a device looks up the array's device address with
 //    cudaGetSymbolAddress (with that device current); make that first call
-//    before any stream capture is begun on the device;
+//    before any stream capture is begun on the device.  The address is kept
+//    until the process exits: a cudaDeviceReset after the first call would
+//    leave it stale, so resetting the device is not supported once this
+//    entry point has been used on it;
 //  * every call shares the one array, so calls whose GPU work overlaps in
 //    time (different streams, different host threads) race and corrupt
 //    each other's results: serialise them;
-//  * the call is synchronous with respect to `stream`, as sky_sort_pairs.
+//  * like sky_sort_pairs, the call returns once the sort has finished: it
+//    reads the error word back and waits for `stream`.
 #include <cuda_runtime.h>
 
 #include <mutex>

@@ -1,5 +1,5 @@
 // Headless viewer render: the reference's frame() path -- preprocess
-// (preprocess.wgsl:116-204), a global depth sort (radix_sort.wgsl), one
+// (preprocess.wgsl:116-215), a global depth sort (radix_sort.wgsl), one
 // screen-space quad per splat (gaussian.wgsl:15-52) blended back to front
 // with src-alpha / one-minus-src-alpha (gaussian-renderer.ts:863-868) into a
 // cleared target -- as CUDA kernels writing an f32 RGBA device buffer.
@@ -22,7 +22,7 @@ SKY_DEV float load_param(const float* P, uint32_t stride, int plane, uint32_t g,
   return r16 ? round_f16(v) : v;
 }
 
-// float_to_ordered_uint (preprocess.wgsl:94-98) of -z_camera: ascending key
+// float_to_ordered_uint (preprocess.wgsl:101-105) of -z_camera: ascending key
 // = far to near.
 SKY_DEV uint32_t ordered_key(float x) {
   const uint32_t bits = __float_as_uint(x);

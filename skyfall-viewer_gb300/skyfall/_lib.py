@@ -34,6 +34,7 @@ BUF = dict(
     records=1, counts=2, cumsum=3, keys_emit=4, keys_sorted=5, vals_sorted=6, flatten=7,
     tile_offsets=8, color=9, alpha=10, last_ids=11, residual=12, partials=13, tile_grads=14,
     grads=15, groups=16, step_scalars=17, depth_radius=18, view_rgba=19, item_order=20,
+    pair_counts=21,
 )
 BUF_DTYPE = dict(
     records=np.float32, counts=np.uint32, cumsum=np.uint32, keys_emit=np.uint32,
@@ -41,6 +42,7 @@ BUF_DTYPE = dict(
     color=np.float32, alpha=np.float32, last_ids=np.uint32, residual=np.float32,
     partials=np.float32, tile_grads=np.int32, grads=np.float32, groups=np.uint32,
     step_scalars=np.float32, depth_radius=np.float32, view_rgba=np.float32, item_order=np.uint32,
+    pair_counts=np.uint64,
 )
 
 ERROR_NAMES = {
@@ -90,7 +92,8 @@ class SkyStatus(C.Structure):
                 ("error_flags", C.c_uint32), ("kernel_launches", C.c_uint64),
                 ("graph_replays", C.c_uint64), ("graph_captures", C.c_uint64),
                 ("scene_extent", C.c_float), ("scored_views", C.c_uint32),
-                ("densify_runs", C.c_uint32), ("prune_runs", C.c_uint32)]
+                ("densify_runs", C.c_uint32), ("prune_runs", C.c_uint32),
+                ("step_h2d_bytes", C.c_uint64), ("step_d2h_bytes", C.c_uint64)]
 
 
 STAGES = ["preprocess", "scan", "emit", "sort", "ranges", "forward", "backward", "geom_adam"]

@@ -46,6 +46,11 @@ def band_extent(a, b, c, mx, my, smax, v0, v1):
     w0, w1 = np.maximum(v0, -V), np.minimum(v1, V)
     vr = np.minimum(np.maximum(v_right, w0), w1)
     vl = np.minimum(np.maximum(-v_right, w0), w1)
+    # a band beyond E's top or bottom row (within the margin): that row's extent
+    beyond = w0 > w1
+    tip = np.where(v0 > 0, V, -V)
+    vr = np.where(beyond, tip, vr)
+    vl = np.where(beyond, tip, vl)
     dr = np.maximum(two_a_l - det * vr * vr, f(0))
     dl = np.maximum(two_a_l - det * vl * vl, f(0))
     ur = (-b * vr + np.sqrt(dr)) / a + u_margin
@@ -145,6 +150,37 @@ def test_row_spans_list_every_reached_tile(ts):
                     assert lo <= tx < lo + n, (i, ty, tx, lo, n)
     assert reached > 1000
     assert listed <= 1.1 * reached
+
+
+def test_bands_beyond_the_extreme_rows_get_the_tip_extent():
+    """A band of rows wholly beyond E's top or bottom row but within the
+    row margin (the f32 rounding allowance) still 'meets' E; its extent is
+    that of the extreme row: it holds the tip -b v / a at v = +-V and every
+    pixel of the band that passes the f32 pre-filter."""
+    rng = np.random.default_rng(31)
+    a, b, c, mx, my, smax = random_splats(rng, 40000, 0, 0)
+    keep = (smax > 0) & (b * b <= f(0.98) * (a * c))
+    a, b, c, mx, my, smax = (x[keep] for x in (a, b, c, mx, my, smax))
+    L = f(1.001) * smax
+    det = a * c - b * b
+    V = np.sqrt(f(2) * a * L / det)
+    vm = f(1.01) * V + f(0.05)
+    for side in (1.0, -1.0):
+        # a one-row band strictly between V and the margin, below or above
+        t = rng.random(a.size).astype(f)
+        vb = (f(side) * (V + (vm - V) * (f(0.05) + f(0.9) * t))).astype(f)
+        beyond = np.abs(vb) > V
+        meets, ul, ur = band_extent(a, b, c, mx, my, smax, vb, vb)
+        assert meets[beyond].all()
+        tipu = -b * (f(side) * V) / a
+        assert ((ul <= tipu) & (tipu <= ur))[beyond].all()
+        # pixels of that row: any that passes the f32 test lies in the extent
+        for du in np.linspace(-40, 40, 161, dtype=f):
+            px, py = mx + du, my + vb
+            s = kernel_s(a, b, c, mx, my, px, py)
+            ok = (s >= 0) & (s <= smax) & beyond
+            rel = px - mx
+            assert not (ok & ((rel < ul) | (rel > ur))).any()
 
 
 def test_ill_conditioned_conics_are_never_dropped():

@@ -42,6 +42,10 @@ def test_noalloc_sort_matches_sky_sort_pairs_twice(sky):
          rng.integers(0, 2**32, 1_000_000, dtype=np.uint64).astype(np.uint32), 32),
         (((rng.integers(0, 8160, 300_001) << 16) | rng.integers(2, 7, 300_001)).astype(np.uint32),
          None, 29),
+        # exactly the maximum (256 full tiles of 4096 keys), a key width that
+        # is not a multiple of 8, with values
+        (rng.integers(0, 2**32, 1 << 20, dtype=np.uint64).astype(np.uint32),
+         rng.integers(0, 2**32, 1 << 20, dtype=np.uint64).astype(np.uint32), 23),
     ]
     for keys, vals, bits in cases:        # two calls in a row through one scratch array
         k_ref, v_ref = run(sky, "sky_sort_pairs", keys, vals, bits)
