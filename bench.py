@@ -69,10 +69,13 @@ def parse():
     ap.add_argument("--no-extras", action="store_true",
                     help="skip matched_loss, mixed, configs and cpu_legs (profiling runs)")
     ap.add_argument("--cpu-sample-views", type=int, default=1)
-    ap.add_argument("--workload", default="train1080", choices=["train1080", "mixed", "stress4k"],
+    ap.add_argument("--workload", default="train1080",
+                    choices=["train1080", "mixed", "stress4k", "train720"],
                     help="train1080: 1M SH-3 clusters, 16 orbit views 1920x1080 per step; "
                          "mixed: 16 views per step of 640x480 / 1280x720 / 1920x1080; "
-                         "stress4k: 4M tightly clustered SH-3 Gaussians, one 3840x2160 view")
+                         "stress4k: 4M tightly clustered SH-3 Gaussians, one 3840x2160 view; "
+                         "train720: a full training run (500k SH-3, 100 Fibonacci cameras "
+                         "1280x720, --steps Adam steps, densify + prune every 100)")
     ap.add_argument("--tile-size", type=int, default=16, choices=[8, 16, 32])
     ap.add_argument("--fwd-batch", type=int, default=0, choices=[0, 64, 128, 256],
                     help="forward splat-batch depth (0 = 256)")
@@ -540,6 +543,75 @@ def gpu_configs(sky, torch, P1080):
     return out
 
 
+def full_training_run(sky, torch, args):
+    """A full training run through the public API: N = 500k Gaussians
+    initialised as the plain-step scene (means U[-1,1]^3, log-scales
+    N(-4, 0.3), logits N(0, 1), DC colours U[0,1]) with SH degree 3 (higher
+    coefficients 0), targets rendered from the separate 300k-Gaussian scene,
+    100 cameras 1280x720 on a Fibonacci sphere of radius 4, `steps` Adam steps
+    of one seeded camera each (the reference's train(n)) with the
+    TrainingController schedule set to densify (with its combined scored
+    prune) every 100 steps from step 100 and prune opacities below 0.005.
+    Device time of the whole run (CUDA events on the library stream);
+    the loss over all 100 cameras before and after."""
+    from skyfall import scenes
+    n = args.n if args.n != 1_000_000 else 500_000
+    P = scenes.scene_uniform(n, seed=1003)
+    cams = scenes.cameras_fibonacci(100, 4.0, 1280, 720)
+    targets = render_targets(sky, cams, args)
+    r = sky.GaussianRenderer(sh_degree=3, sh_degree_interval=0, w_l2=1.0, w_l1=0.2, w_ssim=0.0,
+                             max_views_per_step=max(1, args.views), use_graph=1, tile_size=16)
+    r.load_points(P)
+    r.setTrainingCameras(cams)
+    r.setTrainingImages(targets)
+    r.setTileCull(True)
+    r.setSchedule(densify_from=100, densify_until=args.steps, densify_interval=100,
+                  prune_from=100, prune_until=args.steps, prune_interval=100,
+                  opacity_reset_interval=100000, min_opacity=0.005)
+    px_all = sum(c["width"] * c["height"] for c in cams)
+
+    def loss_all():
+        tot = 0.0
+        for k in range(0, 100, 50):
+            tot += r.forward(list(range(k, k + 50)))
+        return tot / (3 * px_all)
+
+    l0 = loss_all()
+    stream = torch.cuda.ExternalStream(r.stream())
+    r.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    t0 = time.perf_counter()
+    e0.record(stream)
+    r.train(args.steps, views_per_step=max(1, args.views))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ms = e0.elapsed_time(e1)
+    st = r.getStatus()
+    l1 = loss_all()
+    views = args.steps * max(1, args.views)
+    line = {
+        "metric": METRIC, "value": views / (ms / 1000.0), "unit": "iters/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": 0, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"full training run: {n} Gaussians SH-3 (plain-step initialisation), "
+                               f"100 Fibonacci cameras 1280x720 (r = 4), targets rendered from a "
+                               f"{args.gt}-Gaussian scene, {args.steps} Adam steps of "
+                               f"{max(1, args.views)} seeded view(s), densify + scored prune "
+                               f"(min opacity 0.005) every 100 steps",
+                   "tile_size": 16, "tile_cull": True, "schedule": "densify/prune every 100 from 100"},
+        "initial_loss": l0, "final_loss": l1,
+        "loss_def": "sum over the 100 views of 0.5 r^2 + 0.2 |r| per channel, / (3 x pixels)",
+        "gaussians_initial": n, "gaussians_final": int(st.num_gaussians),
+        "densify_runs": int(st.densify_runs), "prune_runs": int(st.prune_runs),
+        "graph_replays": int(st.graph_replays), "seconds_device": ms / 1000.0, "seconds_wall": wall,
+        "device_bytes": int(st.device_bytes),
+    }
+    r.close()
+    print(json.dumps(line))
+    return 0
+
+
 def reference_arm(args):
     """The reference's path timed on the host cores: the oracle port, one
     full view-iteration per step, on the GPU arm's scene, cameras and
@@ -586,6 +658,8 @@ def main():
     import skyfall as sky
     from skyfall import build
     build.build()
+    if args.workload == "train720":
+        return full_training_run(sky, torch, args) if rank == 0 else 0
 
     P, cams = workload(args)
     targets = render_targets(sky, cams, args)

@@ -372,9 +372,11 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches, u
     d2h += sizeof(DevStatus);
     CK(cudaMemcpyAsync(c->h_st, c->d_st.p, sizeof(DevStatus), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    // (after an error the later kernels of the step do nothing, and the
+    // (the capacity bit is the group-bounds kernel's request to grow; after
+    // a sort that gave up the later kernels of the step do nothing and the
     // count is not to be trusted: no growth)
-    if (c->h_st->error == 0u && c->h_st->total_isect > c->icap) {
+    const uint32_t fatal = c->h_st->error & ~SKY_DEVERR_CAPACITY;
+    if (fatal == 0u && c->h_st->total_isect > c->icap) {
       TRY(ensure_isect(c, c->h_st->total_isect));
       b = make_buffers(c);
       c->h_sp->icap = c->icap;
@@ -752,12 +754,15 @@ int score_views(Context* c, const std::vector<uint32_t>& views) {
       const uint32_t npx = vi.width * vi.height;
       const uint32_t blocks = stat_blocks(npx);
       TRY(dev_alloc(c, c->metric_l1, (size_t)npx * 4));
-      // partials: blocks f32 minima, blocks f32 maxima, then (8-byte aligned)
-      // blocks f64 sums
-      TRY(dev_alloc(c, c->metric_part, (size_t)blocks * 16 + 8));
+      // partials: blocks f32 minima, blocks f32 maxima, then blocks f64 sums
+      // at byte offset 8 * blocks of the (256-byte aligned) allocation, so the
+      // f64 array is 8-byte aligned for every block count
+      TRY(dev_alloc(c, c->metric_part, (size_t)blocks * 16));
       float* pmin = (float*)c->metric_part.p;
       float* pmax = pmin + blocks;
-      double* psum = (double*)(pmax + blocks + (blocks & 1));
+      double* psum = (double*)(pmax + blocks);
+      if ((reinterpret_cast<uintptr_t>(psum) & 7u) != 0u)
+        return fail(SKY_ERR_STATE, "metric partials misaligned");
       launch_metric_map(b.color, b.targets, vi.pixel_base, vi.target_base, npx,
                         (float*)c->metric_l1.p, s);
       launch_metric_stats((const float*)c->metric_l1.p, npx, pmin, pmax, psum, blocks, st + v, s);

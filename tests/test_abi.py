@@ -128,3 +128,47 @@ def test_header_is_c99_and_links_from_c(sky, tmp_path):
     assert out.returncode == 0, (out.returncode, out.stderr)
     ver, w, h, sx = out.stdout.split()
     assert (int(ver), int(w), int(h)) == (1, 64, 48) and float(sx) == pytest.approx(2 * 100 / 64, rel=1e-6)
+
+
+NODE_DIR = REPO / "skyfall-viewer_gb300" / "node"
+
+
+def test_napi_addon_type_checks_against_the_napi_declarations():
+    """skyfall_addon.c compiles (syntax and types, -Wall -Wextra -Werror)
+    against a declarations-only stand-in of <node_api.h> and include/skyfall.h:
+    every N-API and sky_* call has the right signature.  (No Node here, so it
+    is not linked or run; tests/test_addon_sequence_gpu.py makes its
+    sequence of library calls on the GPU.)"""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    subprocess.run([cc, "-std=c11", "-fsyntax-only", "-Wall", "-Wextra", "-Werror", "-Wno-unused-parameter",
+                    f"-I{REPO / 'tests' / 'napi_decls'}", f"-I{REPO / 'include'}",
+                    str(NODE_DIR / "skyfall_addon.c")], check=True)
+
+
+def test_facade_calls_only_functions_the_addon_defines():
+    """Every addon.<name>( the TypeScript façade makes is exported by the
+    addon's Init table and declared in its .d.ts, and every sky_* entry point
+    the addon calls is declared in include/skyfall.h."""
+    c_src = (NODE_DIR / "skyfall_addon.c").read_text()
+    exported = set(re.findall(r'FN\("([A-Za-z]+)"', c_src))
+    ts = (NODE_DIR / "skyfall-renderer.ts").read_text()
+    called = set(re.findall(r"\baddon\.([A-Za-z]+)\(", ts))
+    dts = (NODE_DIR / "skyfall_addon.d.ts").read_text()
+    declared = set(re.findall(r"^\s+([A-Za-z]+)\(ctx", dts, flags=re.M)) | {"create"}
+    assert called, "the façade calls the addon"
+    assert called <= exported, sorted(called - exported)
+    assert exported <= declared, sorted(exported - declared)
+    # the reference's GaussianRenderer training methods are all there
+    for name in ("train", "stopTraining", "prune", "resetOpacity", "setTrainingCameras",
+                 "setTrainingImages", "buildTrainingTiles", "initializeKnnAndSync",
+                 "getTrainingParams", "setTrainingParams", "getTrainingStatus", "getGaussianCount",
+                 "getLossWeights", "setLossWeights", "enableProfiling", "printProfilingReport",
+                 "profiledTrainStep", "getSceneExtent", "dumpTrainingDiagnostics",
+                 "setGaussianScale", "resizeViewport", "forward", "backward"):
+        assert re.search(rf"^\s+(async\s+)?{name}\(", ts, flags=re.M), name
+    sky_calls = set(re.findall(r"\b(sky_[a-z0-9_]+)\(", c_src))
+    assert sky_calls <= set(header_functions()), sorted(sky_calls - set(header_functions()))
