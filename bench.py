@@ -94,6 +94,8 @@ def parse():
             args.n = 4_000_000
         args.views = args.cameras = 1
         args.width, args.height = 3840, 2160
+    if args.workload == "train720" and "--views" not in sys.argv:
+        args.views = 1  # the reference's train(n): one view per Adam step
     return args
 
 
@@ -307,14 +309,15 @@ def pair_stats(pairs, steps: int = 1):
     the warps' pixel slots that evaluated a pair."""
     if pairs is None or int(pairs[2]) == 0:
         return None
-    f_eval, f_con, f_ent, b_eval, b_con, b_ent = (int(x) / steps for x in pairs)
+    f_eval, f_con, f_ent, b_eval, b_con, b_ent, b_idle = (int(x) / steps for x in pairs[:7])
     return {
         "forward": {"pairs_evaluated": f_eval, "pairs_contributing": f_con, "warp_entries": f_ent,
                     "lane_use": f_eval / (32.0 * f_ent) if f_ent else None,
                     "contributing_share": f_con / f_eval if f_eval else None},
         "backward": {"pairs_evaluated": b_eval, "pairs_contributing": b_con, "warp_entries": b_ent,
                      "slot_use": b_eval / (64.0 * b_ent) if b_ent else None,
-                     "contributing_share": b_con / b_eval if b_eval else None},
+                     "contributing_share": b_con / b_eval if b_eval else None,
+                     "entries_without_contribution": b_idle / b_ent if b_ent else None},
     }
 
 

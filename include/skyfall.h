@@ -268,13 +268,14 @@ typedef struct SkySchedule {
 #define SKY_BUF_GRADS 15       /* 59 gradient planes of the last backward         */
 #define SKY_BUF_GROUPS 16      /* per sort group: begin, end intersection, u32    */
 #define SKY_BUF_DEPTH_RADIUS 18 /* per (view, Gaussian) camera depth, radius, f32 */
-#define SKY_BUF_PAIR_COUNTS 21  /* 6 u64 of the last pass, counted only at profiling
+#define SKY_BUF_PAIR_COUNTS 21  /* 8 u64 of the last pass, counted only at profiling
                                    level 2 (16x16 tiles, default batch depths):
                                    forward (pixel, splat) pairs evaluated, pairs
                                    composited, warp list entries (32 pixels
                                    each); backward pixel pairs evaluated, pairs
                                    contributing, warp list entries (64 pixels
-                                   each)                                         */
+                                   each), entries at which no pixel of the warp
+                                   contributed; 0                                */
 #define SKY_BUF_STEP_SCALARS 17 /* f32: lr pos, scale, rot, opacity, sh, beta1,
                                    beta2, eps, bias-correction 1/bc1, 1/sqrt(bc2),
                                    SH degree, SH-update flag                     */

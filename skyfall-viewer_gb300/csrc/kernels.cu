@@ -361,47 +361,40 @@ __global__ void k_group_bounds(DevBuffers b) {
 // to one view, so a stable sort of these keys on the tile field alone yields
 // the order of the reference's stable sort of the full keys over (view,
 // Gaussian) emission: within a tile by depth16, ties by Gaussian.
+//
+// One thread per item in item order, so every read is coalesced: the
+// item's tile count, its emission end (scattered into item order by the
+// scan), its depth field (the item key the preprocess wrote), its rectangle
+// and, with culled lists, its record.  Each thread writes its item's
+// contiguous range [end - count, end) of the emission order.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const StepParams& sp = *b.sp;
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t v = blockIdx.y;
   if (g >= sp.n || v >= sp.num_views) return;
-  if (capacity_failed(b.status)) return;  // perm / cumsum are not to be trusted
-  const uint32_t pos = v * sp.n + g;  // position in emission (perm) order
-  // items of one sort group's views interleave: the view is the item's own;
-  // the sorted item key carries its depth field
-  uint32_t item, view, dq, c16 = 0xFFFFu;
-  if (b.perm) {
-    item = b.perm[pos];
-    view = item / sp.n;
-    const uint32_t ik = b.ikeys_sorted[pos];
-    dq = ik & 0xFFFFu;
-    c16 = ik >> 16;
-  } else {
-    item = pos;
-    view = v;
-    dq = depth_key(b.aux[item].x);
+  if (capacity_failed(b.status)) return;  // item_end / cumsum are not to be trusted
+  const uint32_t item = v * sp.n + g;
+  // the rectangle's area, or the culled count when the lists are culled
+  const uint32_t cnt = b.counts[item];
+  if (cnt == 0u) return;
+  const uint32_t end = b.perm ? b.item_end[item] : b.cumsum[item];
+  if (end > sp.icap || cnt > end) {
+    atomicOr(&b.status->error, SKY_DEVERR_LISTS);
+    return;
   }
+  const uint32_t dq = b.ikeys[item] & 0xFFFFu;  // depth16 (depth_key of the item's depth)
   const uint2 rc = b.rects[item];
   const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
-  if (x1 <= x0 || y1 <= y0) return;  // no tiles
-  const uint32_t area = (x1 - x0) * (y1 - y0);
-  // the count is the rectangle's area unless the lists are culled (then the
-  // sorted item key carries it when below 0xFFFF)
-  const uint32_t cnt = !sp.tile_cull ? area : (c16 < 0xFFFFu ? c16 : b.counts[item]);
-  if (cnt == 0u) return;
-  const uint32_t end = b.cumsum[pos];
-  if (end > sp.icap) return;
+  const uint32_t area = (x1 <= x0 || y1 <= y0) ? 0u : (x1 - x0) * (y1 - y0);
   uint32_t cur = end - cnt;
-  const ViewInfo& vi = sp.views[view];
-  const uint32_t it = item;
+  const ViewInfo& vi = sp.views[v];
   if (cnt == area) {
     for (uint32_t ty = y0; ty < y1; ++ty)
       for (uint32_t tx = x0; tx < x1; ++tx) {
         const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
         b.keys[cur] = (kt << 16) | dq;
-        b.rec_of[cur] = it;
+        b.rec_of[cur] = item;
         ++cur;
       }
     return;
@@ -411,7 +404,7 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   const float4 r0 = b.records[(size_t)item * 3 + 0];
   const float cc = b.records[(size_t)item * 3 + 1].x, smax = b.records[(size_t)item * 3 + 2].y;
   EllipseRows e;
-  if (!ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
+  if (!sp.tile_cull || !ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
     atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
     return;
   }
@@ -425,7 +418,7 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
     for (uint32_t tx = lo; tx < lo + len; ++tx) {
       const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
       b.keys[cur] = (kt << 16) | dq;
-      b.rec_of[cur] = it;
+      b.rec_of[cur] = item;
       ++cur;
     }
   }
@@ -436,8 +429,8 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
 // Tile ranges: offsets[t] = first sorted intersection of tile t, empty tiles
 // take the start of the next non-empty one (build_tile_offsets +
 // host backward min-fill, training-tiles.wgsl:250-271 and
-// gaussian-renderer.ts:1966-2020).  Also resolves the item of every sorted
-// intersection.
+// gaussian-renderer.ts:1966-2020).  (The item of every sorted intersection,
+// flatten, is written by the sort's last digit pass.)
 // ---------------------------------------------------------------------------
 // Grid-stride over the step's intersections: the grid is sized for the
 // capacity's order of magnitude, not the capacity itself.
@@ -464,7 +457,6 @@ __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
     }
     if (i + 1 == ge)
       for (uint32_t u = t + 1; u < gi.tile_end; ++u) b.offsets[u] = ge;
-    b.flatten[i] = b.rec_of[b.vals_sorted[i]];
   }
 }
 
@@ -1046,8 +1038,10 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
 // arithmetic is that of k_backward_exact; the per-(tile, intersection) sums
 // differ only in summation order.
 // ---------------------------------------------------------------------------
+// racc = r . acc: the residual dotted with the colour accumulated behind the
+// current splat (starting from the background), the only use of that colour.
 struct BwdPix {
-  float px, py, T, acc[3], r[3];
+  float px, py, T, racc, r[3];
   int hi;
 };
 
@@ -1088,8 +1082,10 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
   const float om = 1.0f - a;  // >= 0.001 (a <= 0.999): the reference's max(1 - a, 1e-4)
   const float Tb = __fdividef(p.T, om);
   const float ctb = a * Tb;
-  const float d0 = q1.z - p.acc[0], d1 = q1.w - p.acc[1], d2 = q2.x - p.acc[2];
-  const float dLda = __fmaf_rn(p.r[2], d2, __fmaf_rn(p.r[1], d1, p.r[0] * d0)) * Tb;
+  // dL/dalpha = r . (colour - acc) T_before, with r . acc carried as racc
+  const float rcol = __fmaf_rn(p.r[2], q2.x, __fmaf_rn(p.r[1], q1.w, p.r[0] * q1.z));
+  const float dd = rcol - p.racc;
+  const float dLda = dd * Tb;
   const float dl = al > MAX_ALPHA ? 0.0f : dLda;
   const float g = dl * al;
   const float gdx = g * dx, gdy = g * dy;
@@ -1102,9 +1098,7 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
   val[6] = __fmaf_rn(gdy, dy, val[6]);
   val[7] = val[7] + gdx;
   val[8] = val[8] + gdy;
-  p.acc[0] = __fmaf_rn(a, d0, p.acc[0]);
-  p.acc[1] = __fmaf_rn(a, d1, p.acc[1]);
-  p.acc[2] = __fmaf_rn(a, d2, p.acc[2]);
+  p.racc = __fmaf_rn(a, dd, p.racc);  // acc += a (colour - acc), dotted with r
   p.T = Tb;
   return true;
 }
@@ -1141,7 +1135,6 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
     p.px = (float)x + 0.5f;
     p.py = (float)y + 0.5f;
     p.T = 1.0f;
-    p.acc[0] = sp.bg[0]; p.acc[1] = sp.bg[1]; p.acc[2] = sp.bg[2];
     p.r[0] = p.r[1] = p.r[2] = 0.0f;
     p.hi = (int)start - 1;
     if (x < vi.width && y < vi.height) {
@@ -1152,6 +1145,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float4 rs = b.residual[q];
       p.r[0] = rs.x; p.r[1] = rs.y; p.r[2] = rs.z;
     }
+    p.racc = __fmaf_rn(p.r[2], sp.bg[2], __fmaf_rn(p.r[1], sp.bg[1], p.r[0] * sp.bg[0]));
   }
   int whi = max(pix[0].hi, pix[1].hi);
 #pragma unroll
@@ -1163,7 +1157,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   const int slot = scatter9_slot(lane);
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
-  uint32_t n_eval = 0, n_contrib = 0, n_entries = 0;  // counting variant only
+  uint32_t n_eval = 0, n_contrib = 0, n_entries = 0, n_idle = 0;  // counting variant only
   // intersections no pixel reaches get zero partials
   for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
     float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
@@ -1214,6 +1208,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
         if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val) || contrib;
       }
       const uint32_t who = __ballot_sync(kFull, contrib);
+      if constexpr (CNT) n_idle += who == 0u ? 1u : 0u;
       if (who == 0u) {
         if (slot < 9) s_part[warp][j][slot] = 0.0f;
       } else if ((who & (who - 1u)) == 0u) {
@@ -1250,8 +1245,12 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
     }
   }
-  // (every lane walks the warp's list: lane 0's n_entries is the warp's)
-  if constexpr (CNT) add_pair_counts(b, 3, n_eval, n_contrib, n_entries);
+  // (every lane walks the warp's list: lane 0's n_entries and n_idle are
+  // the warp's)
+  if constexpr (CNT) {
+    add_pair_counts(b, 3, n_eval, n_contrib, n_entries);
+    if (lane == 0) atomicAdd(&b.status->pairs[6], (unsigned long long)n_idle);
+  }
 }
 
 // ---------------------------------------------------------------------------

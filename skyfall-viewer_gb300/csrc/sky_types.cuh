@@ -67,8 +67,9 @@ struct DevStatus {
   // Work counters of the rasterizers, filled only by their counting variants
   // (profiling level 2): forward (pixel, splat) pairs evaluated, pairs
   // composited, warp list entries; backward pixel pairs evaluated, pairs
-  // contributing, warp list entries (each entry covers 64 pixels).
-  unsigned long long pairs[6];
+  // contributing, warp list entries (each entry covers 64 pixels), entries
+  // at which no pixel of the warp contributed; one spare word.
+  unsigned long long pairs[8];
 };
 
 // Device buffers of a context (all owned by the host runtime).
