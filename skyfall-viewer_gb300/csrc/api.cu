@@ -394,9 +394,8 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches, u
     // keys were emitted in depth order within each tile's items: sorting on
     // the tile field (digits 2 and 3) alone gives the full key order
     SortSegment seg{&dst->group_bounds[g][0], 0};
-    // the last digit pass also writes flatten[i] = rec_of[vals_sorted[i]]
     CK(sort_pairs_launch(b.keys, nullptr, b.keys_sorted, b.vals_sorted, seg, c->icap, sh.key_bits[g],
-                         c->sort, &dst->error, s, 2, true, b.rec_of, b.flatten));
+                         c->sort, &dst->error, s, 2, true));
     launches += 2 + (sh.key_bits[g] + 7) / 8 - 2;
   }
   TRY(mark(4));

@@ -429,8 +429,8 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
 // Tile ranges: offsets[t] = first sorted intersection of tile t, empty tiles
 // take the start of the next non-empty one (build_tile_offsets +
 // host backward min-fill, training-tiles.wgsl:250-271 and
-// gaussian-renderer.ts:1966-2020).  (The item of every sorted intersection,
-// flatten, is written by the sort's last digit pass.)
+// gaussian-renderer.ts:1966-2020).  Also resolves the item of every sorted
+// intersection.
 // ---------------------------------------------------------------------------
 // Grid-stride over the step's intersections: the grid is sized for the
 // capacity's order of magnitude, not the capacity itself.
@@ -457,6 +457,7 @@ __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
     }
     if (i + 1 == ge)
       for (uint32_t u = t + 1; u < gi.tile_end; ++u) b.offsets[u] = ge;
+    b.flatten[i] = b.rec_of[b.vals_sorted[i]];
   }
 }
 

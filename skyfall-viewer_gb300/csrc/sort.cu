@@ -158,8 +158,7 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
            int pass, int passes, int digit_lo, const uint32_t* __restrict__ trivial, uint32_t key_bits,
            const uint32_t* __restrict__ hist, uint32_t* __restrict__ tile_counter,
            uint32_t* __restrict__ lookback, uint32_t max_tiles, uint32_t* __restrict__ err,
-           uint32_t spin_limit, uint32_t withhold_tile0, const uint32_t* __restrict__ gather_src,
-           uint32_t* __restrict__ gather_dst) {
+           uint32_t spin_limit, uint32_t withhold_tile0) {
   __shared__ uint32_t s_keys[kSortTile];
   __shared__ uint32_t s_vals[kSortTile];
   __shared__ uint32_t s_warp_hist[kWarps][kRadix];
@@ -196,9 +195,6 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
   const uint32_t* __restrict__ vals_in = j == 0 ? vals_src : buf_of(j - 1, false);
   uint32_t* __restrict__ keys_out = buf_of(j, true);
   uint32_t* __restrict__ vals_out = buf_of(j, false);
-  // the last pass that moves keys also writes gather_src[value] per output
-  // position (the item of each sorted intersection), when asked to
-  uint32_t* __restrict__ gdst = (j == m - 1) ? gather_dst : nullptr;
 
   uint32_t begin, n;
   seg_bounds(seg, begin, n);
@@ -320,7 +316,6 @@ k_onesweep(const uint32_t* keys_src, const uint32_t* vals_src, uint32_t* keys_ds
     }
     keys_out[begin + gp] = kk;
     vals_out[begin + gp] = s_vals[i];
-    if (gdst) gdst[begin + gp] = gather_src[s_vals[i]];
   }
   }  // next tile
 }
@@ -372,7 +367,7 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
                               uint32_t* err, cudaStream_t stream, int digit_lo,
-                              bool fault_point, const uint32_t* gather_src, uint32_t* gather_dst) {
+                              bool fault_point) {
   if (key_bits == 0) key_bits = 1;
   if (key_bits > 32) key_bits = 32;
   const int passes = (int)((key_bits + 7) / 8);
@@ -401,8 +396,7 @@ cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                                                     sc.keys_tmp, sc.vals_tmp, seg, p, passes,
                                                     digit_lo, trivial, key_bits, sc.hist,
                                                     sc.tile_counter, sc.lookback, sc.max_tiles, err,
-                                                    spin_limit, inject ? 1u : 0u, gather_src,
-                                                    gather_dst);
+                                                    spin_limit, inject ? 1u : 0u);
   return cudaGetLastError();
 }
 

@@ -57,16 +57,11 @@ struct SortSegment {
 // fault_point: the sort counts for SKY_FAULT=lookback:N (host fault
 // injection, used by tests); only callers whose later kernels check the
 // error word before indexing with the sort's output pass true.
-// gather_src / gather_dst (optional, both or neither): the last digit pass
-// also writes gather_dst[p] = gather_src[vals_out[p]] for every output
-// position p of the segment (vals_in must be NULL or indices into
-// gather_src).
 cudaError_t sort_pairs_launch(const uint32_t* keys_in, const uint32_t* vals_in,
                               uint32_t* keys_out, uint32_t* vals_out, SortSegment seg,
                               uint32_t max_n, uint32_t key_bits, const SortScratch& sc,
                               uint32_t* err, cudaStream_t stream, int digit_lo = 0,
-                              bool fault_point = false, const uint32_t* gather_src = nullptr,
-                              uint32_t* gather_dst = nullptr);
+                              bool fault_point = false);
 
 // Host fault injection (SKY_FAULT=lookback:N, api.cu): true for the N-th
 // fault-point sort launched outside graph capture in the process.  Without
