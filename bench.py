@@ -407,25 +407,28 @@ def matched_loss(sky, torch, P, args, ts: int):
     both reach.  Both use SH degree 3 from the start, SH planes updated every
     step and no position-learning-rate warm-up: the reference's schedules
     count steps, which would give the plain trainer 16x the warm-up
-    progress."""
+    progress.  The batched trainer runs twice: with batch-scaled Adam
+    hyperparameters (SkyConfig.batch_scaling: learning rates x sqrt(16),
+    betas^16; the headline ratio) and with those of one view."""
     from skyfall import scenes
     cams = scenes.cameras_mixed(16, 5.0)
     targets = render_targets(sky, cams, args)
     px_all = sum(c["width"] * c["height"] for c in cams)
     epochs = 40
 
-    def make(graph):
+    def make(graph, scaling=0):
         r = sky.GaussianRenderer(sh_degree=3, sh_degree_interval=0, sh_update_interval=1,
                                  lr_means_delay_mult=1.0, w_l2=1.0, w_l1=0.2, w_ssim=0.0,
-                                 max_views_per_step=16, use_graph=graph, tile_size=ts)
+                                 max_views_per_step=16, use_graph=graph, tile_size=ts,
+                                 batch_scaling=scaling)
         r.load_points(P)
         r.setTrainingCameras(cams)
         r.setTrainingImages(targets)
         r.setTileCull(True)
         return r
 
-    def run(batched):
-        r = make(1 if batched else 0)
+    def run(batched, scaling=0):
+        r = make(1 if batched else 0, scaling)
         stream = torch.cuda.ExternalStream(r.stream())
         rng = np.random.default_rng(77)
         curve = [(0.0, r.forward(list(range(16))) / (3 * px_all))]
@@ -445,21 +448,34 @@ def matched_loss(sky, torch, P, args, ts: int):
         r.close()
         return curve
 
-    cb = run(True)
+    cb = run(True, 1)
+    cu = run(True, 0)
     cp = run(False)
-    level = max(min(l for _, l in cb), min(l for _, l in cp))
-    tb, tp = interp_time(cb, level), interp_time(cp, level)
+
+    def at_matched(c):
+        level = max(min(l for _, l in c), min(l for _, l in cp))
+        tb, tp = interp_time(c, level), interp_time(cp, level)
+        return level, tb, tp, ((tp / tb) if (tb and tp) else None)
+
+    level, tb, tp, ratio = at_matched(cb)
+    ulevel, utb, utp, uratio = at_matched(cu)
     return {
         "cameras": "16 on a Fibonacci sphere, 640x480 / 1280x720 / 1920x1080",
         "views_each": epochs * 16, "tile_size": ts,
         "loss": "sum over the 16 views of 0.5 r^2 + 0.2 |r| per channel, / (3 x pixels)",
         "initial_loss": cb[0][1],
-        "batched": {"final_loss": cb[-1][1], "seconds": cb[-1][0], "adam_steps": epochs},
+        "batched": {"final_loss": cb[-1][1], "seconds": cb[-1][0], "adam_steps": epochs,
+                    "adam": "batch_scaling 1: learning rates x 4, betas^16"},
         "plain": {"final_loss": cp[-1][1], "seconds": cp[-1][0], "adam_steps": epochs * 16},
         "common_loss": level,
         "batched_seconds_to_common_loss": tb, "plain_seconds_to_common_loss": tp,
-        "batched_over_plain_at_matched_loss": (tp / tb) if (tb and tp) else None,
-        "curves": {"batched": [[round(a, 5), b] for a, b in cb], "plain": [[round(a, 5), b] for a, b in cp]},
+        "batched_over_plain_at_matched_loss": ratio,
+        "unscaled": {"adam": "batch_scaling 0: one view's hyperparameters", "final_loss": cu[-1][1],
+                     "common_loss": ulevel, "batched_seconds_to_common_loss": utb,
+                     "plain_seconds_to_common_loss": utp, "batched_over_plain_at_matched_loss": uratio},
+        "curves": {"batched": [[round(a, 5), b] for a, b in cb],
+                   "batched_unscaled": [[round(a, 5), b] for a, b in cu],
+                   "plain": [[round(a, 5), b] for a, b in cp]},
     }
 
 

@@ -121,6 +121,15 @@ typedef struct SkyConfig {
                                   are the shorter lists.  Renders, forward
                                   passes and the reference backward mode
                                   always list every tile.  Default 0.        */
+  uint32_t batch_scaling;      /* Adam hyperparameters of a step of B views.
+                                  0: those of one view, whatever B (the
+                                  reference trains one view per step).
+                                  1: the learning rates times sqrt(B), beta1
+                                  and beta2 raised to the power B, bias
+                                  correction counted in views (the batch
+                                  rule of Zhao et al. 2024, "On Scaling Up
+                                  3D Gaussian Splatting Training"); steps of
+                                  one view are unchanged.  Default 0.        */
 } SkyConfig;
 
 typedef struct SkyStepStats {

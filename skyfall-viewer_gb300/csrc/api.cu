@@ -174,6 +174,7 @@ struct Context {
   StepParams* h_sp = nullptr;
   DevStatus* h_st = nullptr;
   uint64_t iteration = 0, adam_steps = 0, last_isect = 0;
+  uint64_t adam_views = 0;  // views summed over the Adam steps taken
   double last_loss = 0.0;
   uint64_t rng = 0;
   size_t device_bytes = 0;
@@ -576,7 +577,21 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   sp.importance_decay = 0.98f;  // DEFAULT_IMPORTANCE_CONFIG.decay (importance.ts:9)
   {
     // run_adam_on_buffer (gaussian-renderer.ts:2420-2430): t = max(1, counter)
-    const double t = (double)std::max<uint64_t>(1, c->adam_steps);
+    double t = (double)std::max<uint64_t>(1, c->adam_steps);
+    if (cfg.batch_scaling && nv > 1) {
+      // a step of B views: learning rates x sqrt(B), betas to the power B;
+      // the bias correction's exponent counts views (max(B, views so far)
+      // is t = max(1, counter) in view units, so B = 1 steps are unchanged)
+      const double sq = std::sqrt((double)nv);
+      sp.lr_pos = (float)(position_lr(cfg, it) * sq);
+      sp.lr_scale = (float)(js_literal(cfg.lr_scale) * sq);
+      sp.lr_rot = (float)(js_literal(cfg.lr_rotation) * sq);
+      sp.lr_opacity = (float)(js_literal(cfg.lr_opacity) * sq);
+      sp.lr_sh = (float)(js_literal(cfg.lr_sh) * sq);
+      sp.beta1 = (float)std::pow(js_literal(cfg.beta1), (double)nv);
+      sp.beta2 = (float)std::pow(js_literal(cfg.beta2), (double)nv);
+    }
+    if (cfg.batch_scaling) t = (double)std::max<uint64_t>(nv, c->adam_views);
     const double bc1 = 1.0 - std::pow(js_literal(cfg.beta1), t);
     const double bc2 = 1.0 - std::pow(js_literal(cfg.beta2), t);
     sp.bc1_rcp = (float)(1.0 / bc1);
@@ -674,6 +689,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   if (mode == kTrain) {
     c->iteration = it;
     c->adam_steps += 1;
+    c->adam_views += nv;
     c->warm_steps += 1;
   }
   if (stats) {
@@ -1111,6 +1127,8 @@ static int check_cfg(const SkyConfig* cfg) {
   if (cfg->bwd_batch != 0 && cfg->bwd_batch != 32 && cfg->bwd_batch != 64 && cfg->bwd_batch != 128)
     return fail(SKY_ERR_ARG, "bwd_batch %u not in {0, 32, 64, 128}", cfg->bwd_batch);
   if (cfg->tile_cull > 1) return fail(SKY_ERR_ARG, "tile_cull %u not 0 or 1", cfg->tile_cull);
+  if (cfg->batch_scaling > 1)
+    return fail(SKY_ERR_ARG, "batch_scaling %u not 0 or 1", cfg->batch_scaling);
   return SKY_OK;
 }
 
@@ -1221,6 +1239,7 @@ static int load_planes(Context* c, uint32_t n) {
   c->stride = stride;
   c->iteration = 0;
   c->adam_steps = 0;
+  c->adam_views = 0;
   c->fwd_ready = false;
   c->scores_valid = false;
   c->scores_n = 0;
@@ -1346,7 +1365,8 @@ struct CkptHeader {
   uint32_t version, n, planes, reserved0;
   uint64_t iteration, adam_steps, rng;
   float scene_extent;
-  uint32_t densify_runs, prune_runs, reserved1;
+  uint32_t densify_runs, prune_runs;
+  uint32_t adam_views;  // saturating; 0 in files written before it was kept
 };
 }  // namespace
 
@@ -1366,6 +1386,7 @@ int sky_save_checkpoint(void* p, const char* path) {
   h.scene_extent = c->scene_extent;
   h.densify_runs = c->densify_runs;
   h.prune_runs = c->prune_runs;
+  h.adam_views = (uint32_t)std::min<uint64_t>(c->adam_views, 0xFFFFFFFFu);
   std::vector<float> P((size_t)kPlanes * n), M1(P.size()), M2(P.size()), I4((size_t)n * 4), G4(I4.size());
   TRY(sky_get_params(p, P.data(), n));
   TRY(sky_get_moments(p, M1.data(), M2.data(), n));
@@ -1411,6 +1432,7 @@ int sky_load_checkpoint(void* p, const char* path) {
   CK(cudaStreamSynchronize(s));
   c->iteration = h.iteration;
   c->adam_steps = h.adam_steps;
+  c->adam_views = h.adam_views ? h.adam_views : h.adam_steps;
   c->rng = h.rng;
   c->scene_extent = h.scene_extent;
   c->densify_runs = h.densify_runs;

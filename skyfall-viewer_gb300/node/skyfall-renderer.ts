@@ -206,6 +206,8 @@ export class SkyfallRenderer {
   /** splat-batch depths and culled lists: speed only, results unchanged */
   setBatchDepth(fwdBatch = 0, bwdBatch = 0): void { addon.setConfig(this.ctx, { fwdBatch, bwdBatch }); }
   setTileCull(on = true): void { addon.setConfig(this.ctx, { tileCull: on ? 1 : 0 }); }
+  /** Adam hyperparameters of multi-view steps: lr x sqrt(B), betas^B (one-view steps unchanged) */
+  setBatchScaling(on = true): void { addon.setConfig(this.ctx, { batchScaling: on ? 1 : 0 }); }
 
   // ---- profiling (TrainingProfiler) ------------------------------------------
   enableProfiling(enabled: boolean): void { addon.setProfiling(this.ctx, enabled ? 1 : 0); }

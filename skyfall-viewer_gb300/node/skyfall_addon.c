@@ -216,7 +216,8 @@ static int apply_config(napi_env env, napi_value o, SkyConfig* c) {
          opt_uint(env, o, "sh_update_interval", &c->sh_update_interval) &&
          opt_float(env, o, "w_l2", &c->w_l2) && opt_float(env, o, "w_l1", &c->w_l1) &&
          opt_float(env, o, "w_ssim", &c->w_ssim) && opt_uint(env, o, "fwdBatch", &c->fwd_batch) &&
-         opt_uint(env, o, "bwdBatch", &c->bwd_batch) && opt_uint(env, o, "tileCull", &c->tile_cull);
+         opt_uint(env, o, "bwdBatch", &c->bwd_batch) && opt_uint(env, o, "tileCull", &c->tile_cull) &&
+         opt_uint(env, o, "batchScaling", &c->batch_scaling);
 }
 
 /* create({tileSize, shDegree, useGraph, maxViewsPerStep, seed, ...config}?) */
@@ -278,6 +279,7 @@ static napi_value GetConfig(napi_env env, napi_callback_info info) {
   set_num(env, o, "fwdBatch", c.fwd_batch);
   set_num(env, o, "bwdBatch", c.bwd_batch);
   set_num(env, o, "tileCull", c.tile_cull);
+  set_num(env, o, "batchScaling", c.batch_scaling);
   set_num(env, o, "tileSize", c.tile_size);
   set_num(env, o, "shDegree", c.sh_degree);
   return o;

@@ -27,6 +27,8 @@ export interface AddonConfig {
   sh_update_interval?: number;
   w_l2?: number; w_l1?: number; w_ssim?: number;
   fwdBatch?: number; bwdBatch?: number; tileCull?: number;
+  /** 1: a step of B views scales the learning rates by sqrt(B) and the betas to the power B */
+  batchScaling?: number;
 }
 
 export interface CreateOptions extends AddonConfig {

@@ -76,6 +76,7 @@ class SkyConfig(C.Structure):
         ("round_params_f16", C.c_uint32), ("backward_mode", C.c_uint32), ("use_graph", C.c_uint32),
         ("max_views_per_step", C.c_uint32), ("seed", C.c_uint64),
         ("fwd_batch", C.c_uint32), ("bwd_batch", C.c_uint32), ("tile_cull", C.c_uint32),
+        ("batch_scaling", C.c_uint32),
     ]
 
 

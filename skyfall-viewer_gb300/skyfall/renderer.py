@@ -338,6 +338,14 @@ class GaussianRenderer:
         self.config.tile_cull = 1 if on else 0
         L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
 
+    def setBatchScaling(self, on: bool) -> None:
+        """Adam hyperparameters of a step of B views: off, those of one view
+        (the reference's); on, learning rates x sqrt(B) and betas to the
+        power B (Zhao et al. 2024), bias correction counted in views.  Steps
+        of one view are unchanged either way."""
+        self.config.batch_scaling = 1 if on else 0
+        L.check(self._L.sky_set_config(self._h, C.byref(self.config)))
+
     def getLossWeights(self) -> LossWeights:
         return LossWeights(self.config.w_l2, self.config.w_l1, self.config.w_ssim)
 

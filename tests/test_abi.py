@@ -59,6 +59,11 @@ def test_config_size_is_checked_before_touching_the_device(sky):
     c = sky.default_config(tile_cull=2)
     assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
     assert b"tile_cull" in L.sky_last_error()
+    # batch-scaled Adam hyperparameters: a switch, off by default
+    assert sky.default_config().batch_scaling == 0
+    c = sky.default_config(batch_scaling=2)
+    assert L.sky_create(C.byref(c), C.byref(h)) == sky._lib.SKY_ERR_ARG
+    assert b"batch_scaling" in L.sky_last_error()
 
 
 def test_pinhole_camera_matches_reference_projection(sky):
