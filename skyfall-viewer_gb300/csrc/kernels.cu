@@ -70,21 +70,43 @@ struct EllipseRows {
   float v_right;      // -b U / c
 };
 
+// Square root and quotient of the ellipse arithmetic.  The tile lists use the
+// IEEE operations, so the preprocess's counts and the emission's tiles agree
+// bit for bit.  The rasterisers' per-block masks only have to be
+// conservative: they take sqrt.approx (relative error below 2^-22) and the
+// fast reciprocal division (2 ulp), errors far inside the margins above.
+template <bool Fast>
+SKY_DEV float e_sqrt(float x) {
+  if constexpr (Fast) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+  } else {
+    return sqrtf(x);
+  }
+}
+template <bool Fast>
+SKY_DEV float e_div(float x, float y) {
+  if constexpr (Fast) return __fdividef(x, y);
+  else return x / y;
+}
+
+template <bool Fast = false>
 SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float smax, EllipseRows& r) {
   if (!(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c)) || !(smax > 0.0f)) return false;
   const float L = 1.001f * smax;
   const float det = a * c - bq * bq;
-  const float U = sqrtf(2.0f * c * L / det);
+  const float U = e_sqrt<Fast>(e_div<Fast>(2.0f * c * L, det));
   r.mx = mx;
   r.my = my;
   r.a = a;
   r.b = bq;
   r.det = det;
   r.two_a_l = 2.0f * a * L;
-  r.V = sqrtf(r.two_a_l / det);
+  r.V = e_sqrt<Fast>(e_div<Fast>(r.two_a_l, det));
   r.v_margin = 1.01f * r.V + 0.05f;
   r.u_margin = 0.01f * U + 0.05f;
-  r.v_right = -bq * U / c;
+  r.v_right = e_div<Fast>(-bq * U, c);
   return true;
 }
 
@@ -102,6 +124,7 @@ SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float 
 // row but within v_margin of it (w0 > w1) can only hold pixels that pass
 // through that rounding, within 1e-5 V of the extreme row, so it gets the
 // extent of that row (the tip -b v / a at v = +-V, plus the margins).
+template <bool Fast = false>
 SKY_DEV bool band_extent(const EllipseRows& r, float v0, float v1, float& ul, float& ur) {
   if (v1 < -r.v_margin || v0 > r.v_margin) return false;
   const float w0 = fmaxf(v0, -r.V), w1 = fminf(v1, r.V);
@@ -114,8 +137,8 @@ SKY_DEV bool band_extent(const EllipseRows& r, float v0, float v1, float& ul, fl
   }
   const float dr = fmaxf(r.two_a_l - r.det * vr * vr, 0.0f);
   const float dl = fmaxf(r.two_a_l - r.det * vl * vl, 0.0f);
-  ur = (-r.b * vr + sqrtf(dr)) / r.a + r.u_margin;
-  ul = (-r.b * vl - sqrtf(dl)) / r.a - r.u_margin;
+  ur = e_div<Fast>(-r.b * vr + e_sqrt<Fast>(dr), r.a) + r.u_margin;
+  ul = e_div<Fast>(-r.b * vl - e_sqrt<Fast>(dl), r.a) - r.u_margin;
   return true;
 }
 
@@ -523,14 +546,14 @@ SKY_DEV uint32_t ellipse_band_mask(float4 r0, float4 r1, float4 r2, uint32_t x0,
   constexpr int NCOL = TS / BW, NROW = TS / BH;
   const uint32_t m = block_mask<TS, BW, BH>(r0, r2, x0, y0);
   EllipseRows e;
-  if (m == 0u || !ellipse_rows(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
+  if (m == 0u || !ellipse_rows<true>(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
   uint32_t keep = 0u;
 #pragma unroll 1
   for (int br = 0; br < NROW; ++br) {
     if (((m >> (br * NCOL)) & ((1u << NCOL) - 1u)) == 0u) continue;
     const float cy = (float)(y0 + (uint32_t)(br * BH)) + 0.5f;
     float ul, ur;
-    if (!band_extent(e, cy - e.my, (cy + (float)(BH - 1)) - e.my, ul, ur)) continue;
+    if (!band_extent<true>(e, cy - e.my, (cy + (float)(BH - 1)) - e.my, ul, ur)) continue;
     const float xl = e.mx + ul, xr = e.mx + ur;
 #pragma unroll
     for (int bc = 0; bc < NCOL; ++bc) {
@@ -1054,19 +1077,36 @@ SKY_DEV float exp_neg_approx(float s) {
   return r;
 }
 
-// One (pixel, splat) pair of the exact backward: adds the pair's nine raw
-// moments to val and steps the pixel's transmittance and accumulated colour
-// back past the splat.  Returns whether the splat contributes at the pixel.
+// The s below which a pair surely contributes, unclamped: for a splat with
+// opacity <= 0.9989 (alpha = opacity exp(-s) rounds to at most 0.99890018 <
+// 0.999, never clamped) it is the raster pre-filter bound smax =
+// __logf(255 opacity) + 1e-3 less 1.1e-3.  smax - 1e-3 is within 2e-6 of
+// ln(opacity / f32(1/255)) (3 ulp of __logf, f32 roundings), so at s <=
+// smax - 1.1e-3 the exact alpha is at least f32(1/255) (1 + 9e-5), far
+// beyond the forward exponential's 1-ulp error: the forward composited the
+// pair.  -1 (no pair is sure) for opacities that can reach the clamp.
+SKY_DEV float sure_bound(const float4& q1, const float4& q2) {
+  return q1.y > 0.9989f ? -1.0f : q2.y - 1.1e-3f;
+}
+
+// One (pixel, splat) pair of the exact backward: adds the pair's raw moments
+// to val and steps the pixel's transmittance and accumulated colour back past
+// the splat.  val[0..3] are the colour-weighted and opacity moments; since
+// a lane's two pixels share dx, val[4..6] hold sum g, sum g dy and sum g dy^2
+// (g = dL/dalpha alpha), and the entry forms g dx^2, g dx dy, g dy^2, g dx,
+// g dy from them (lane_moments).  Returns whether the splat contributes at the pixel.
 // Which pairs contribute (alpha >= 1/255) and which are clamped (alpha >
 // 0.999) must be decided exactly as the forward decided them; the gradient
-// values only have to be accurate.  So alpha comes from the fast exponential,
+// values only have to be accurate.  A pair with s <= s_sure (sure_bound)
+// contributes unclamped; above it, alpha comes from the fast exponential,
 // and from sky_expf (the forward's) only when it lies within 2e-6 relative of
-// either threshold, where the two could decide differently.
+// either threshold, where the two could decide differently.  In both cases
+// the gradient uses the fast exponential's alpha.
 // dx = px - mx, s1 = (a/2 dx) dx (q0, q1 are staged records, conic halved)
 // and bdx = b dx belong to the pixel column and are shared by the lane's two
 // pixels.
 SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0, const float4& q1,
-                      const float4& q2, float val[9]) {
+                      const float4& q2, float s_sure, float val[9]) {
   const float dy = p.py - q0.y;
   const float s2 = (q1.x * dy) * dy;  // staged record: halved conic
   float so2 = s1 + s2;
@@ -1074,12 +1114,17 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
   if (outside_smax(so2, q2.y)) return false;
   float G = exp_neg_approx(so2);
   float al = q1.y * G;
-  if (fabsf(al - MIN_ALPHA) <= 2e-6f * MIN_ALPHA || fabsf(al - MAX_ALPHA) <= 2e-6f) {
-    G = sky_expf_inrange(-so2);
-    al = q1.y * G;
+  float a = al;
+  bool clamped = false;
+  if (so2 > s_sure) {
+    if (fabsf(al - MIN_ALPHA) <= 2e-6f * MIN_ALPHA || fabsf(al - MAX_ALPHA) <= 2e-6f) {
+      G = sky_expf_inrange(-so2);
+      al = q1.y * G;
+    }
+    a = fmin_(al, MAX_ALPHA);
+    if (!(a >= MIN_ALPHA)) return false;
+    clamped = al > MAX_ALPHA;  // the clamp has zero slope
   }
-  const float a = fmin_(al, MAX_ALPHA);
-  if (!(a >= MIN_ALPHA)) return false;
   const float om = 1.0f - a;  // >= 0.001 (a <= 0.999): the reference's max(1 - a, 1e-4)
   const float Tb = __fdividef(p.T, om);
   const float ctb = a * Tb;
@@ -1087,21 +1132,30 @@ SKY_DEV bool bwd_pair(BwdPix& p, float dx, float s1, float bdx, const float4& q0
   const float rcol = __fmaf_rn(p.r[2], q2.x, __fmaf_rn(p.r[1], q1.w, p.r[0] * q1.z));
   const float dd = rcol - p.racc;
   const float dLda = dd * Tb;
-  const float dl = al > MAX_ALPHA ? 0.0f : dLda;
+  const float dl = clamped ? 0.0f : dLda;
   const float g = dl * al;
-  const float gdx = g * dx, gdy = g * dy;
+  const float gdy = g * dy;
   val[0] = __fmaf_rn(p.r[0], ctb, val[0]);
   val[1] = __fmaf_rn(p.r[1], ctb, val[1]);
   val[2] = __fmaf_rn(p.r[2], ctb, val[2]);
   val[3] = __fmaf_rn(dl, a, val[3]);
-  val[4] = __fmaf_rn(gdx, dx, val[4]);
-  val[5] = __fmaf_rn(gdx, dy, val[5]);
-  val[6] = __fmaf_rn(gdy, dy, val[6]);
-  val[7] = val[7] + gdx;
-  val[8] = val[8] + gdy;
+  val[4] = val[4] + g;                     // sum g      (dx is the lane's)
+  val[5] = val[5] + gdy;                   // sum g dy
+  val[6] = __fmaf_rn(gdy, dy, val[6]);     // sum g dy^2
   p.racc = __fmaf_rn(a, dd, p.racc);  // acc += a (colour - acc), dotted with r
   p.T = Tb;
   return true;
+}
+
+// The nine moments of a lane from its accumulators (bwd_pair) and its dx.
+SKY_DEV void lane_moments(float val[9], float dx) {
+  const float gs = val[4], gy = val[5], gyy = val[6];
+  const float gdx = gs * dx;
+  val[4] = gdx * dx;
+  val[5] = gy * dx;
+  val[6] = gyy;
+  val[7] = gdx;
+  val[8] = gy;
 }
 
 // BB: the splat-batch depth (32, 64 or 128 staged splats); the per-splat sums
@@ -1174,8 +1228,10 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float4 q0 = b.records[r * 3 + 0];
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
-      stage_record(s_rec + k * 3, q0, q1, q2);
       s_mask[k] = ellipse_band_mask<TS, 8, 8>(q0, q1, q2, tx * TS, ty * TS);
+      // the box half-widths are only needed for the mask: the staged record
+      // carries the splat's sure bound in their place
+      stage_record(s_rec + k * 3, q0, q1, make_float4(q2.x, q2.y, sure_bound(q1, q2), q2.w));
     }
     __syncthreads();
     uint32_t nlist = 0;
@@ -1196,18 +1252,20 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float4 q0 = s_rec[j * 3 + 0], q1 = s_rec[j * 3 + 1], q2 = s_rec[j * 3 + 2];
       const float dx = pix[0].px - q0.x;
       const float s1 = (q0.z * dx) * dx, bdx = q0.w * dx;
+      const float s_sure = q2.z;  // sure_bound, staged
       bool contrib = false;
       if constexpr (CNT) {
         ++n_entries;
         bool c0 = false, c1 = false;
-        if (i <= pix[0].hi) { ++n_eval; c0 = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, val); }
-        if (i <= pix[1].hi) { ++n_eval; c1 = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val); }
+        if (i <= pix[0].hi) { ++n_eval; c0 = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, s_sure, val); }
+        if (i <= pix[1].hi) { ++n_eval; c1 = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, s_sure, val); }
         n_contrib += (uint32_t)c0 + (uint32_t)c1;
         contrib = c0 || c1;
       } else {
-        if (i <= pix[0].hi) contrib = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, val);
-        if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, val) || contrib;
+        if (i <= pix[0].hi) contrib = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, s_sure, val);
+        if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, s_sure, val) || contrib;
       }
+      lane_moments(val, dx);
       const uint32_t who = __ballot_sync(kFull, contrib);
       if constexpr (CNT) n_idle += who == 0u ? 1u : 0u;
       if (who == 0u) {
