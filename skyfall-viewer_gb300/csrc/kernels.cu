@@ -70,43 +70,35 @@ struct EllipseRows {
   float v_right;      // -b U / c
 };
 
-// Square root and quotient of the ellipse arithmetic.  The tile lists use the
-// IEEE operations, so the preprocess's counts and the emission's tiles agree
-// bit for bit.  The rasterisers' per-block masks only have to be
-// conservative: they take sqrt.approx (relative error below 2^-22) and the
-// fast reciprocal division (2 ulp), errors far inside the margins above.
-template <bool Fast>
+// Square root and quotient of the ellipse arithmetic.  Tile lists and
+// per-block masks only have to be conservative, so they take sqrt.approx
+// (relative error below 2^-22) and the fast reciprocal division (2 ulp),
+// errors far inside the margins above (the CPU tests check the extents with
+// every square root and quotient moved adversarially by 2e-6).  The
+// preprocess's counts and the emission's tiles come from the same code, so
+// they agree bit for bit.
 SKY_DEV float e_sqrt(float x) {
-  if constexpr (Fast) {
-    float r;
-    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-  } else {
-    return sqrtf(x);
-  }
+  float r;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
-template <bool Fast>
-SKY_DEV float e_div(float x, float y) {
-  if constexpr (Fast) return __fdividef(x, y);
-  else return x / y;
-}
+SKY_DEV float e_div(float x, float y) { return __fdividef(x, y); }
 
-template <bool Fast = false>
 SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float smax, EllipseRows& r) {
   if (!(a > 0.0f) || !(c > 0.0f) || !(bq * bq <= 0.98f * (a * c)) || !(smax > 0.0f)) return false;
   const float L = 1.001f * smax;
   const float det = a * c - bq * bq;
-  const float U = e_sqrt<Fast>(e_div<Fast>(2.0f * c * L, det));
+  const float U = e_sqrt(e_div(2.0f * c * L, det));
   r.mx = mx;
   r.my = my;
   r.a = a;
   r.b = bq;
   r.det = det;
   r.two_a_l = 2.0f * a * L;
-  r.V = e_sqrt<Fast>(e_div<Fast>(r.two_a_l, det));
+  r.V = e_sqrt(e_div(r.two_a_l, det));
   r.v_margin = 1.01f * r.V + 0.05f;
   r.u_margin = 0.01f * U + 0.05f;
-  r.v_right = e_div<Fast>(-bq * U, c);
+  r.v_right = e_div(-bq * U, c);
   return true;
 }
 
@@ -124,7 +116,6 @@ SKY_DEV bool ellipse_rows(float mx, float my, float a, float bq, float c, float 
 // row but within v_margin of it (w0 > w1) can only hold pixels that pass
 // through that rounding, within 1e-5 V of the extreme row, so it gets the
 // extent of that row (the tip -b v / a at v = +-V, plus the margins).
-template <bool Fast = false>
 SKY_DEV bool band_extent(const EllipseRows& r, float v0, float v1, float& ul, float& ur) {
   if (v1 < -r.v_margin || v0 > r.v_margin) return false;
   const float w0 = fmaxf(v0, -r.V), w1 = fminf(v1, r.V);
@@ -137,8 +128,8 @@ SKY_DEV bool band_extent(const EllipseRows& r, float v0, float v1, float& ul, fl
   }
   const float dr = fmaxf(r.two_a_l - r.det * vr * vr, 0.0f);
   const float dl = fmaxf(r.two_a_l - r.det * vl * vl, 0.0f);
-  ur = e_div<Fast>(-r.b * vr + e_sqrt<Fast>(dr), r.a) + r.u_margin;
-  ul = e_div<Fast>(-r.b * vl - e_sqrt<Fast>(dl), r.a) - r.u_margin;
+  ur = e_div(-r.b * vr + e_sqrt(dr), r.a) + r.u_margin;
+  ul = e_div(-r.b * vl - e_sqrt(dl), r.a) - r.u_margin;
   return true;
 }
 
@@ -153,8 +144,8 @@ SKY_DEV uint32_t row_span(const EllipseRows& r, uint32_t ty, uint32_t x0, uint32
   if (!band_extent(r, v0, v1, ul, ur)) return 0u;
   // tiles whose centre columns [tx ts + 0.5, tx ts + ts - 0.5] meet [mx + ul, mx + ur]
   const float fts = (float)ts;
-  const float t_lo = ceilf(((r.mx + ul) - (fts - 0.5f)) / fts);
-  const float t_hi = floorf(((r.mx + ur) - 0.5f) / fts);
+  const float t_lo = ceilf(e_div((r.mx + ul) - (fts - 0.5f), fts));
+  const float t_hi = floorf(e_div((r.mx + ur) - 0.5f, fts));
   const float flo = fmaxf(t_lo, (float)x0), fhi = fminf(t_hi, (float)x1 - 1.0f);
   if (!(fhi >= flo)) return 0u;
   lo = (uint32_t)flo;
@@ -184,8 +175,8 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
     smax = smax_g;
     if (smax > 0.0f) {
       const float sb = 2.0f * (1.25f * smax + 0.01f);
-      hx = sqrtf(sb * o.cov00) + 0.01f;
-      hy = sqrtf(sb * o.cov11) + 0.01f;
+      hx = e_sqrt(sb * o.cov00) + 0.01f;  // (only masks read the box: 25 % margin)
+      hy = e_sqrt(sb * o.cov11) + 0.01f;
     }
   }
   float4* rec = b.records + item * 3;
@@ -546,14 +537,14 @@ SKY_DEV uint32_t ellipse_band_mask(float4 r0, float4 r1, float4 r2, uint32_t x0,
   constexpr int NCOL = TS / BW, NROW = TS / BH;
   const uint32_t m = block_mask<TS, BW, BH>(r0, r2, x0, y0);
   EllipseRows e;
-  if (m == 0u || !ellipse_rows<true>(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
+  if (m == 0u || !ellipse_rows(r0.x, r0.y, r0.z, r0.w, r1.x, r2.y, e)) return m;
   uint32_t keep = 0u;
 #pragma unroll 1
   for (int br = 0; br < NROW; ++br) {
     if (((m >> (br * NCOL)) & ((1u << NCOL) - 1u)) == 0u) continue;
     const float cy = (float)(y0 + (uint32_t)(br * BH)) + 0.5f;
     float ul, ur;
-    if (!band_extent<true>(e, cy - e.my, (cy + (float)(BH - 1)) - e.my, ul, ur)) continue;
+    if (!band_extent(e, cy - e.my, (cy + (float)(BH - 1)) - e.my, ul, ur)) continue;
     const float xl = e.mx + ul, xr = e.mx + ur;
 #pragma unroll
     for (int bc = 0; bc < NCOL; ++bc) {
@@ -618,7 +609,7 @@ SKY_DEV void add_pair_counts(const DevBuffers& b, int base, uint32_t eval, uint3
 // evaluates and composites and the list entries its warps walk; the
 // arithmetic and every result are those of the plain variant.
 template <int TS, int FB, bool CNT = false>
-__global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
+__global__ void __launch_bounds__(TS* TS, TS == 16 ? 6 : 1) k_forward(DevBuffers b) {
   static_assert(FB <= 256, "list entries are bytes");
   constexpr int NT = TS * TS;
   constexpr int NW = NT / 32;
@@ -659,7 +650,7 @@ __global__ void __launch_bounds__(TS* TS) k_forward(DevBuffers b) {
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
       stage_record(s_rec + k * 3, q0, q1, q2);
-      s_mask[k] = block_mask<TS, 8, 4>(q0, q2, tx * TS, ty * TS);
+      s_mask[k] = ellipse_band_mask<TS, 8, 4>(q0, q1, q2, tx * TS, ty * TS);
     }
     __syncthreads();
     // this warp's splats of the batch, in order (skipped splats cannot pass

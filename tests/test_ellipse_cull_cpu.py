@@ -12,7 +12,10 @@ arithmetic (ellipse_rows, band_extent, ellipse_band_mask and row_span in
 kernels.cu) in numpy, one rounding per operation, and check it against the
 rasterisers' own f32 evaluation of s at every pixel centre, on random splats
 with anisotropy up to the conditioning limit (b^2 <= 0.98 a c) and means on
-both sides of the edges.
+both sides of the edges.  The kernels evaluate the extents' square roots and
+quotients with sqrt.approx and the fast division (relative errors below
+2^-22); the tests run the restatement exact and with every square root and
+quotient moved by a relative 2e-6 in the direction that narrows the extent.
 """
 import numpy as np
 import pytest
@@ -30,18 +33,31 @@ def kernel_s(a, b, c, mx, my, px, py):
     return so2 + (b * dx) * dy
 
 
-def band_extent(a, b, c, mx, my, smax, v0, v1):
+def down(x, rel):
+    """x moved by the relative amount rel towards -inf (an approximate
+    square root or quotient at its worst for a narrowing extent)."""
+    return (x - f(rel) * np.abs(x)).astype(f) if rel else x
+
+
+def up(x, rel):
+    return (x + f(rel) * np.abs(x)).astype(f) if rel else x
+
+
+def band_extent(a, b, c, mx, my, smax, v0, v1, rel=0.0, vr_sign=1.0):
     """ellipse_rows + band_extent (kernels.cu) in f32, elementwise: whether
     the band of pixel-centre rows with dy in [v0, v1] meets the ellipse, and
-    its x-extent [ul, ur] relative to the mean there (margins included)."""
+    its x-extent [ul, ur] relative to the mean there (margins included).
+    rel > 0 perturbs every square root and quotient adversarially (vr_sign
+    picks the direction of the edge maximum's abscissa)."""
     L = f(1.001) * smax
     det = a * c - b * b
-    U = np.sqrt(f(2) * c * L / det)
+    U = down(np.sqrt(down(f(2) * c * L / det, rel)), rel)
     two_a_l = f(2) * a * L
-    V = np.sqrt(two_a_l / det)
+    V = down(np.sqrt(down(two_a_l / det, rel)), rel)
     v_margin = f(1.01) * V + f(0.05)
     u_margin = f(0.01) * U + f(0.05)
     v_right = -b * U / c
+    v_right = (up(v_right, rel) if vr_sign > 0 else down(v_right, rel)) if rel else v_right
     meets = ~((v1 < -v_margin) | (v0 > v_margin))
     w0, w1 = np.maximum(v0, -V), np.minimum(v1, V)
     vr = np.minimum(np.maximum(v_right, w0), w1)
@@ -53,17 +69,18 @@ def band_extent(a, b, c, mx, my, smax, v0, v1):
     vl = np.where(beyond, tip, vl)
     dr = np.maximum(two_a_l - det * vr * vr, f(0))
     dl = np.maximum(two_a_l - det * vl * vl, f(0))
-    ur = (-b * vr + np.sqrt(dr)) / a + u_margin
-    ul = (-b * vl - np.sqrt(dl)) / a - u_margin
+    ur = down((-b * vr + down(np.sqrt(dr), rel)) / a, rel) + u_margin
+    ul = up((-b * vl - down(np.sqrt(dl), rel)) / a, rel) - u_margin
     return meets, ul, ur
 
 
-def block_dropped(a, b, c, mx, my, smax, x0, y0, bw, bh):
+def block_dropped(a, b, c, mx, my, smax, x0, y0, bw, bh, rel=0.0, vr_sign=1.0):
     """ellipse_band_mask's decision for one bw x bh block at (x0, y0)."""
     cond = (a > 0) & (c > 0) & (b * b <= f(0.98) * (a * c)) & (smax > 0)
     with np.errstate(invalid="ignore", divide="ignore"):
         cy = f(y0) + f(0.5)
-        meets, ul, ur = band_extent(a, b, c, mx, my, smax, cy - my, (cy + f(bh - 1)) - my)
+        meets, ul, ur = band_extent(a, b, c, mx, my, smax, cy - my, (cy + f(bh - 1)) - my,
+                                    rel, vr_sign)
         xl, xr = mx + ul, mx + ur
         cx = f(x0) + f(0.5)
         kept = meets & (xr >= cx) & (xl <= cx + f(bw - 1))
@@ -87,16 +104,20 @@ def random_splats(rng, n, x0, y0):
     return a, b, c, mx, my, smax
 
 
-def test_dropped_blocks_hold_no_pixel_within_smax():
+@pytest.mark.parametrize("rel,vr_sign,bw,bh", [(0.0, 1.0, 8, 8), (2e-6, 1.0, 8, 8), (2e-6, -1.0, 8, 8),
+                                              (2e-6, 1.0, 8, 4), (2e-6, -1.0, 8, 4)])
+def test_dropped_blocks_hold_no_pixel_within_smax(rel, vr_sign, bw, bh):
+    """8x8 blocks (backward) and 8x4 blocks (forward), exact and with the
+    approximate operations' worst case."""
     rng = np.random.default_rng(11)
     total_dropped = 0
     for x0, y0 in ((0, 0), (1000, 500), (3832, 2152)):
         a, b, c, mx, my, smax = random_splats(rng, 60000, x0, y0)
         live = smax > 0
-        drop = block_dropped(a, b, c, mx, my, smax, x0, y0, 8, 8) & live
+        drop = block_dropped(a, b, c, mx, my, smax, x0, y0, bw, bh, rel, vr_sign) & live
         reach = np.zeros_like(drop)
-        for yy in range(8):
-            for xx in range(8):
+        for yy in range(bh):
+            for xx in range(bw):
                 s = kernel_s(a, b, c, mx, my, f(x0 + xx) + f(0.5), f(y0 + yy) + f(0.5))
                 reach |= (s >= 0) & (s <= smax)
         assert not (drop & reach).any()
@@ -106,24 +127,25 @@ def test_dropped_blocks_hold_no_pixel_within_smax():
     assert total_dropped > 50000
 
 
-def row_span(a, b, c, mx, my, smax, ty, x0, x1, ts):
+def row_span(a, b, c, mx, my, smax, ty, x0, x1, ts, rel=0.0, vr_sign=1.0):
     """row_span (kernels.cu) in f32: the listed tiles [lo, lo + len) of tile
     row ty of the rectangle [x0, x1)."""
     cy = f(ty * ts) + f(0.5)
-    meets, ul, ur = band_extent(a, b, c, mx, my, smax, cy - my, (cy + f(ts - 1)) - my)
+    meets, ul, ur = band_extent(a, b, c, mx, my, smax, cy - my, (cy + f(ts - 1)) - my, rel, vr_sign)
     if not meets:
         return x0, 0
     fts = f(ts)
-    t_lo = np.ceil(((mx + ul) - (fts - f(0.5))) / fts)
-    t_hi = np.floor(((mx + ur) - f(0.5)) / fts)
+    t_lo = np.ceil(up(((mx + ul) - (fts - f(0.5))) / fts, rel))
+    t_hi = np.floor(down(((mx + ur) - f(0.5)) / fts, rel))
     flo, fhi = max(t_lo, f(x0)), min(t_hi, f(x1 - 1))
     if not fhi >= flo:
         return x0, 0
     return int(flo), int(fhi) - int(flo) + 1
 
 
-@pytest.mark.parametrize("ts", [8, 16, 32])
-def test_row_spans_list_every_reached_tile(ts):
+@pytest.mark.parametrize("ts,rel,vr_sign", [(8, 0.0, 1.0), (16, 0.0, 1.0), (32, 0.0, 1.0),
+                                             (16, 2e-6, 1.0), (16, 2e-6, -1.0), (8, 2e-6, 1.0)])
+def test_row_spans_list_every_reached_tile(ts, rel, vr_sign):
     """The culled intersection lists: per tile row of a Gaussian's rectangle,
     the analytic span of its ellipse must hold every tile with a pixel whose
     f32 s passes the pre-filter, and list few tiles beyond those."""
@@ -138,7 +160,7 @@ def test_row_spans_list_every_reached_tile(ts):
         x0, x1 = int(np.floor((mx[i] - rad) / ts)), int(np.ceil((mx[i] + rad) / ts))
         y0, y1 = int(np.floor((my[i] - rad) / ts)), int(np.ceil((my[i] + rad) / ts))
         for ty in range(y0, y1):
-            lo, n = row_span(a[i], b[i], c[i], mx[i], my[i], smax[i], ty, x0, x1, ts)
+            lo, n = row_span(a[i], b[i], c[i], mx[i], my[i], smax[i], ty, x0, x1, ts, rel, vr_sign)
             listed += n
             ys = f(ty * ts) + f(0.5) + np.arange(ts, dtype=f)
             for tx in range(x0, x1):
