@@ -137,7 +137,7 @@ def algo_bytes(stage: str, n: int, B: int, isect: float, pix: float) -> float:
         "emit": isect * 8 + B * n * 20,
         "sort": isect * 36,
         "ranges": isect * 4,
-        "forward": isect * 52 + pix * 60,
+        "forward": isect * 60 + pix * 60,
         "backward": isect * 100 + pix * 28,
         "geom_adam": n * 1652 + isect * 48,
     }[stage]

@@ -1730,6 +1730,11 @@ int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* siz
   if (!dst || sz == 0) return SKY_OK;
   if (bytes < sz) return fail(SKY_ERR_ARG, "destination holds %llu bytes, need %llu",
                               (unsigned long long)bytes, (unsigned long long)sz);
+  if (which == SKY_BUF_FLATTEN) {
+    // the step resolved only the staged batches; complete it for the reader
+    launch_flatten_fill(make_buffers(c), (uint32_t)I, c->stream);
+    CK(cudaGetLastError());
+  }
   CK(cudaStreamSynchronize(c->stream));
   if (rows)
     CK(cudaMemcpy2D(dst, row_bytes, src, pitch_src, row_bytes, rows, cudaMemcpyDeviceToHost));

@@ -443,35 +443,80 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
 // Tile ranges: offsets[t] = first sorted intersection of tile t, empty tiles
 // take the start of the next non-empty one (build_tile_offsets +
 // host backward min-fill, training-tiles.wgsl:250-271 and
-// gaussian-renderer.ts:1966-2020).  Also resolves the item of every sorted
-// intersection.
+// gaussian-renderer.ts:1966-2020).
+//
+// The item of each sorted intersection (flatten[i] = rec_of[vals_sorted[i]])
+// is resolved by the forward as it stages a batch: every later reader in the
+// exact mode (backward, multi-view scores) stays within each tile's staged
+// batches, since a pixel's last contributor lies in them.  The
+// reference-mode backward walks every list to its end, so for it this kernel
+// resolves them all; a read-back of the buffer completes it (flatten_fill).
 // ---------------------------------------------------------------------------
-// Grid-stride over the step's intersections: the grid is sized for the
-// capacity's order of magnitude, not the capacity itself.
+// Grid-stride over chunks of four sorted intersections (one 16-byte key
+// load; the key before the chunk comes from the cache line the neighbouring
+// thread loaded); the grid is sized for the capacity's order of magnitude,
+// not the capacity itself.  The sort groups' bounds and tile ranges are read
+// once per block into shared memory.
 __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
+  __shared__ uint32_t s_gb[kMaxGroups][2];
+  __shared__ uint32_t s_gt[kMaxGroups][2];
   const StepParams& sp = *b.sp;
   if (capacity_failed(b.status)) return;
+  const int ng = (int)sp.num_groups;
+  for (int k = (int)threadIdx.x; k < ng; k += (int)blockDim.x) {
+    s_gb[k][0] = b.status->group_bounds[k][0];
+    s_gb[k][1] = b.status->group_bounds[k][1];
+    s_gt[k][0] = sp.groups[k].tile_begin;
+    s_gt[k][1] = sp.groups[k].tile_end;
+  }
+  __syncthreads();
   const uint32_t total = min(b.status->total_isect, sp.icap);
-  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-    int g = 0;
-    for (int k = 0; k < (int)sp.num_groups; ++k)
-      if (b.status->group_bounds[k][0] <= i && i < b.status->group_bounds[k][1]) g = k;
-    const GroupInfo& gi = sp.groups[g];
-    const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
-    const uint32_t t = gi.tile_begin + (b.keys_sorted[i] >> 16);
-    if (t >= gi.tile_end || (i > gb && gi.tile_begin + (b.keys_sorted[i - 1] >> 16) > t)) {
-      atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // unsorted or corrupt keys
-      return;
-    }
-    if (i == gb) {
-      for (uint32_t u = gi.tile_begin; u <= t; ++u) b.offsets[u] = i;
+  const bool resolve = sp.bwd_mode != 0;
+  const uint32_t chunks = (total + 3u) / 4u;
+  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < chunks; c += gridDim.x * blockDim.x) {
+    const uint32_t i0 = 4u * c;
+    uint32_t kk[4];
+    if (i0 + 4u <= total) {
+      const uint4 v = reinterpret_cast<const uint4*>(b.keys_sorted)[c];
+      kk[0] = v.x; kk[1] = v.y; kk[2] = v.z; kk[3] = v.w;
     } else {
-      const uint32_t tp = gi.tile_begin + (b.keys_sorted[i - 1] >> 16);
-      for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) kk[j] = i0 + (uint32_t)j < total ? b.keys_sorted[i0 + j] : 0u;
     }
-    if (i + 1 == ge)
-      for (uint32_t u = t + 1; u < gi.tile_end; ++u) b.offsets[u] = ge;
-    b.flatten[i] = b.rec_of[b.vals_sorted[i]];
+    uint32_t prev = i0 > 0u ? b.keys_sorted[i0 - 1u] : 0u;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const uint32_t i = i0 + (uint32_t)j;
+      if (i >= total) break;
+      int g = 0;
+      for (int k = 0; k < ng; ++k)
+        if (s_gb[k][0] <= i && i < s_gb[k][1]) g = k;
+      const uint32_t gb = s_gb[g][0], ge = s_gb[g][1], tb = s_gt[g][0], te = s_gt[g][1];
+      const uint32_t t = tb + (kk[j] >> 16);
+      const uint32_t tp = tb + (prev >> 16);  // the key before, when in the group (i > gb)
+      prev = kk[j];
+      if (t >= te || (i > gb && tp > t)) {
+        atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // unsorted or corrupt keys
+        return;
+      }
+      if (i == gb) {
+        for (uint32_t u = tb; u <= t; ++u) b.offsets[u] = i;
+      } else {
+        for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
+      }
+      if (i + 1 == ge)
+        for (uint32_t u = t + 1; u < te; ++u) b.offsets[u] = ge;
+      if (resolve) b.flatten[i] = b.rec_of[b.vals_sorted[i]];
+    }
+  }
+}
+
+// flatten[i] = rec_of[vals_sorted[i]] for every sorted intersection of the
+// last step (the forward resolved only its staged batches); idempotent.
+__global__ void __launch_bounds__(256) k_flatten_fill(DevBuffers b, uint32_t total) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const uint32_t e = b.vals_sorted[i];
+    if (e < total) b.flatten[i] = b.rec_of[e];
   }
 }
 
@@ -645,7 +690,10 @@ __global__ void __launch_bounds__(TS* TS, TS == 16 ? 6 : 1) k_forward(DevBuffers
     const uint32_t cnt = min((uint32_t)FB, end - bs);
     __syncthreads();
     for (uint32_t k = tid; k < cnt; k += NT) {
-      const size_t r = b.flatten[bs + k];
+      // the batch's items, resolved here for the later readers (k_ranges)
+      const uint32_t item = b.rec_of[b.vals_sorted[bs + k]];
+      b.flatten[bs + k] = item;
+      const size_t r = item;
       const float4 q0 = b.records[r * 3 + 0];
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
@@ -1486,7 +1534,9 @@ SKY_DEV void geom_view(const float pc[4], const ProjOut& o, const ViewInfo& vi, 
   float clip[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) clip[r] = mat4_row(vi.proj, r, pc[0], pc[1], pc[2], pc[3]);
-  const float rw = 1.0f / clip[3];
+  // (gradient arithmetic only -- no decision depends on it -- so quotients
+  // take the fast reciprocal: 2 ulp)
+  const float rw = __fdividef(1.0f, clip[3]);
   const float ndx = clip[0] * rw, ndy = clip[1] * rw;
   const float gx = in9[7] * (0.5f * (float)vi.width) * rw, gy = in9[8] * (0.5f * (float)vi.height) * rw;
 #pragma unroll
@@ -1510,11 +1560,13 @@ SKY_DEV void geom_view(const float pc[4], const ProjOut& o, const ViewInfo& vi, 
 #pragma unroll
     for (int c = 0; c < 2; ++c) Wm[a][c] = tmp[a][0] * V3[c][0] + tmp[a][1] * V3[c][1] + tmp[a][2] * V3[c][2];
   const float tz = pc[2];
-  const float kx = vi.focal[0] / tz, ky = vi.focal[1] / tz;
+  const float rtz = __fdividef(1.0f, tz);
+  const float kx = vi.focal[0] * rtz, ky = vi.focal[1] * rtz;
   const float C00 = kx * kx * Wm[0][0], C01 = kx * ky * Wm[0][1], C11 = ky * ky * Wm[1][1];
   const float e00 = C00 + sp.eps2d, e11 = C11 + sp.eps2d;
   const float det = e00 * e11 - C01 * C01;
-  const float Qa = e11 / det, Qb = -C01 / det, Qc = e00 / det;
+  const float rdet = __fdividef(1.0f, det);
+  const float Qa = e11 * rdet, Qb = -C01 * rdet, Qc = e00 * rdet;
   const float ga = in9[4], gb = 0.5f * in9[5], gc = in9[6];
   // dC = -Q GQ Q (2x2 symmetric)
   const float t00 = ga * Qa + gb * Qb, t01 = ga * Qb + gb * Qc;
@@ -1525,7 +1577,7 @@ SKY_DEV void geom_view(const float pc[4], const ProjOut& o, const ViewInfo& vi, 
   const float dC11 = -(Qb * t01 + Qc * t11);
   const float dC01 = dC01a + dC10a;
   const float dW00 = dC00 * kx * kx, dW01 = dC01 * kx * ky, dW11 = dC11 * ky * ky;
-  dpc[2] += -2.0f / tz * (dC00 * C00 + dC01 * C01 + dC11 * C11);
+  dpc[2] += -2.0f * rtz * (dC00 * C00 + dC01 * C01 + dC11 * C11);
   // G3 = V3^T GW V3 with GW = [[dW00, dW01/2, 0], [dW01/2, dW11, 0], [0, 0, 0]]
   const float hW01 = 0.5f * dW01;
   float u0[3], u1[3];  // GW V3, rows 0 and 1
@@ -1575,11 +1627,11 @@ SKY_DEV void geom_view(const float pc[4], const ProjOut& o, const ViewInfo& vi, 
       addk(14, SH_C3_5 * 2.f * X * Z, SH_C3_5 * (-2.f * Yv * Z), SH_C3_5 * (xx - yy));
       addk(15, SH_C3_6 * (3.f * xx - 3.f * yy), SH_C3_6 * (-6.f * X * Yv), 0.f);
     }
-    float vl = sqrtf(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
+    const float rvl = rsqrtf(pc[0] * pc[0] + pc[1] * pc[1] + pc[2] * pc[2]);
     const float dd = X * ddir[0] + Yv * ddir[1] + Z * ddir[2];
-    dpc[0] += -(ddir[0] - X * dd) / vl;
-    dpc[1] += -(ddir[1] - Yv * dd) / vl;
-    dpc[2] += -(ddir[2] - Z * dd) / vl;
+    dpc[0] += -(ddir[0] - X * dd) * rvl;
+    dpc[1] += -(ddir[1] - Yv * dd) * rvl;
+    dpc[2] += -(ddir[2] - Z * dd) * rvl;
   }
 #pragma unroll
   for (int j = 0; j < 3; ++j) gr.pos[j] += V3[0][j] * dpc[0] + V3[1][j] * dpc[1] + V3[2][j] * dpc[2];
@@ -1932,10 +1984,16 @@ void launch_emit(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s
 
 void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s) {
   if (icap) {
-    const uint32_t blocks = min((icap + 255) / 256, (uint32_t)sm_count() * 16);
+    const uint32_t blocks = min((icap / 4 + 255) / 256 + 1, (uint32_t)sm_count() * 8);
     k_ranges<<<blocks, 256, 0, s>>>(b);
   }
   k_ranges_empty<<<1, 256, 0, s>>>(b);
+}
+
+void launch_flatten_fill(const DevBuffers& b, uint32_t total, cudaStream_t s) {
+  if (!total) return;
+  const uint32_t blocks = min((total + 255) / 256, (uint32_t)sm_count() * 16);
+  k_flatten_fill<<<blocks, 256, 0, s>>>(b, total);
 }
 
 template <int TS>
