@@ -453,10 +453,14 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
 // resolves them all; a read-back of the buffer completes it (flatten_fill).
 // ---------------------------------------------------------------------------
 // Grid-stride over chunks of four sorted intersections (one 16-byte key
-// load; the key before the chunk comes from the cache line the neighbouring
-// thread loaded); the grid is sized for the capacity's order of magnitude,
-// not the capacity itself.  The sort groups' bounds and tile ranges are read
-// once per block into shared memory.
+// load where the chunk lies inside the group; the key before the chunk comes
+// from the cache line the neighbouring thread loaded); the grid is sized for
+// the capacity's order of magnitude, not the capacity itself.  The sort
+// groups' bounds and tile ranges are read once per block into shared memory,
+// and each group's chunks are walked within its bounds (a chunk straddling
+// two groups is split).  Each group writes offsets[tile_end], the end of its
+// last tile (the next group writes the same value there, the start of its
+// first; the last group's is the final sentinel).
 __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
   __shared__ uint32_t s_gb[kMaxGroups][2];
   __shared__ uint32_t s_gt[kMaxGroups][2];
@@ -470,43 +474,46 @@ __global__ void __launch_bounds__(256) k_ranges(DevBuffers b) {
     s_gt[k][1] = sp.groups[k].tile_end;
   }
   __syncthreads();
-  const uint32_t total = min(b.status->total_isect, sp.icap);
   const bool resolve = sp.bwd_mode != 0;
-  const uint32_t chunks = (total + 3u) / 4u;
-  for (uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < chunks; c += gridDim.x * blockDim.x) {
-    const uint32_t i0 = 4u * c;
-    uint32_t kk[4];
-    if (i0 + 4u <= total) {
-      const uint4 v = reinterpret_cast<const uint4*>(b.keys_sorted)[c];
-      kk[0] = v.x; kk[1] = v.y; kk[2] = v.z; kk[3] = v.w;
-    } else {
-#pragma unroll
-      for (int j = 0; j < 4; ++j) kk[j] = i0 + (uint32_t)j < total ? b.keys_sorted[i0 + j] : 0u;
-    }
-    uint32_t prev = i0 > 0u ? b.keys_sorted[i0 - 1u] : 0u;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const uint32_t i = i0 + (uint32_t)j;
-      if (i >= total) break;
-      int g = 0;
-      for (int k = 0; k < ng; ++k)
-        if (s_gb[k][0] <= i && i < s_gb[k][1]) g = k;
-      const uint32_t gb = s_gb[g][0], ge = s_gb[g][1], tb = s_gt[g][0], te = s_gt[g][1];
-      const uint32_t t = tb + (kk[j] >> 16);
-      const uint32_t tp = tb + (prev >> 16);  // the key before, when in the group (i > gb)
-      prev = kk[j];
-      if (t >= te || (i > gb && tp > t)) {
-        atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // unsorted or corrupt keys
-        return;
-      }
-      if (i == gb) {
-        for (uint32_t u = tb; u <= t; ++u) b.offsets[u] = i;
+  for (int g = 0; g < ng; ++g) {
+    const uint32_t gb = s_gb[g][0], ge = s_gb[g][1], tb = s_gt[g][0], te = s_gt[g][1];
+    if (gb >= ge) continue;  // empty: k_ranges_empty
+    const uint32_t c_lo = gb / 4u, c_hi = (ge + 3u) / 4u;
+    for (uint32_t c = c_lo + blockIdx.x * blockDim.x + threadIdx.x; c < c_hi;
+         c += gridDim.x * blockDim.x) {
+      const uint32_t i0 = 4u * c;
+      uint32_t kk[4];
+      if (i0 >= gb && i0 + 4u <= ge) {
+        const uint4 v = reinterpret_cast<const uint4*>(b.keys_sorted)[c];
+        kk[0] = v.x; kk[1] = v.y; kk[2] = v.z; kk[3] = v.w;
       } else {
-        for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const uint32_t i = i0 + (uint32_t)j;
+          kk[j] = (i >= gb && i < ge) ? b.keys_sorted[i] : 0u;
+        }
       }
-      if (i + 1 == ge)
-        for (uint32_t u = t + 1; u < te; ++u) b.offsets[u] = ge;
-      if (resolve) b.flatten[i] = b.rec_of[b.vals_sorted[i]];
+      uint32_t prev = i0 > gb ? b.keys_sorted[i0 - 1u] : 0u;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const uint32_t i = i0 + (uint32_t)j;
+        if (i < gb || i >= ge) continue;
+        const uint32_t t = tb + (kk[j] >> 16);
+        const uint32_t tp = tb + (prev >> 16);  // the key before, when in the group (i > gb)
+        prev = kk[j];
+        if (t >= te || (i > gb && tp > t)) {
+          atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // unsorted or corrupt keys
+          return;
+        }
+        if (i == gb) {
+          for (uint32_t u = tb; u <= t; ++u) b.offsets[u] = i;
+        } else {
+          for (uint32_t u = tp + 1; u <= t; ++u) b.offsets[u] = i;
+        }
+        if (i + 1 == ge)
+          for (uint32_t u = t + 1; u <= te; ++u) b.offsets[u] = ge;
+        if (resolve) b.flatten[i] = b.rec_of[b.vals_sorted[i]];
+      }
     }
   }
 }
@@ -520,7 +527,8 @@ __global__ void __launch_bounds__(256) k_flatten_fill(DevBuffers b, uint32_t tot
   }
 }
 
-// Empty groups and the final sentinel offsets[num_tiles] = total.
+// Empty groups: every tile's range, and the group's offsets[tile_end], start
+// at the group's bound.
 __global__ void k_ranges_empty(DevBuffers b) {
   const StepParams& sp = *b.sp;
   if (capacity_failed(b.status)) return;
@@ -528,10 +536,9 @@ __global__ void k_ranges_empty(DevBuffers b) {
     const uint32_t gb = b.status->group_bounds[g][0], ge = b.status->group_bounds[g][1];
     if (gb != ge) continue;
     const GroupInfo& gi = sp.groups[g];
-    for (uint32_t u = gi.tile_begin + threadIdx.x; u < gi.tile_end; u += blockDim.x)
+    for (uint32_t u = gi.tile_begin + threadIdx.x; u <= gi.tile_end; u += blockDim.x)
       b.offsets[u] = gb;
   }
-  if (threadIdx.x == 0) b.offsets[sp.num_tiles] = min(b.status->total_isect, sp.icap);
 }
 
 // ---------------------------------------------------------------------------
