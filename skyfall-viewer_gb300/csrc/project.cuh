@@ -184,9 +184,11 @@ SKY_DEV bool project_gaussian(Get get, const GaussCov3& gc, const ViewInfo& vi,
   o.my = (0.5f * (ndc_y + 1.0f)) * (float)vi.height;
   o.radius = radius;
   o.depth = depth;
-  const float ts = (float)sp.tile_size;
-  const float tile_x = o.mx / ts, tile_y = o.my / ts;
-  const float trx = radius / ts;
+  // ts is 8, 16 or 32: multiplying by its exact reciprocal is the IEEE
+  // quotient bit for bit, without three division sequences
+  const float rts = 1.0f / (float)sp.tile_size;
+  const float tile_x = o.mx * rts, tile_y = o.my * rts;
+  const float trx = radius * rts;
   o.x0 = min(wgsl_u32(floorf(tile_x - trx)), vi.tiles_x);
   o.y0 = min(wgsl_u32(floorf(tile_y - trx)), vi.tiles_y);
   o.x1 = min(wgsl_u32(ceilf(tile_x + trx)), vi.tiles_x);
