@@ -236,8 +236,15 @@ __global__ void __launch_bounds__(kPrepThreads, 8) k_preprocess(DevBuffers b) {
   float prm[11];
 #pragma unroll
   for (int k = 0; k < 11; ++k) prm[k] = load_plane(b.params, stride, k, g, r16);
-  for (int k = 0; k < 48; ++k)
-    s_sh[k][t] = k < nsh ? load_plane(b.params, stride, 11 + k, g, r16) : 0.0f;
+  // 4 loads in flight at a time (a loop of load, then store, waits on each)
+#pragma unroll
+  for (int k0 = 0; k0 < 48; k0 += 4) {
+    float v[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) v[j] = k0 + j < nsh ? load_plane(b.params, stride, 11 + k0 + j, g, r16) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 4; ++j) s_sh[k0 + j][t] = v[j];
+  }
   auto get = [&](int plane) { return plane < 11 ? prm[plane] : s_sh[plane - 11][t]; };
   // the covariance, opacity and skip bound do not depend on the view
   GaussCov3 gc;
@@ -382,23 +389,32 @@ __global__ void k_group_bounds(DevBuffers b) {
 // and, with culled lists, its record.  Each thread writes its item's
 // contiguous range [end - count, end) of the emission order.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
+__global__ void __launch_bounds__(256, 6) k_emit(DevBuffers b) {
   const StepParams& sp = *b.sp;
   const uint32_t g = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t v = blockIdx.y;
   if (g >= sp.n || v >= sp.num_views) return;
   if (capacity_failed(b.status)) return;  // item_end / cumsum are not to be trusted
   const uint32_t item = v * sp.n + g;
-  // the rectangle's area, or the culled count when the lists are culled
-  const uint32_t cnt = b.counts[item];
-  if (cnt == 0u) return;
+  // every load the item needs is issued before the first branch, so their
+  // latencies overlap (most items are emitted)
+  const uint32_t cnt = b.counts[item];  // the rectangle's area, or the culled count
   const uint32_t end = b.perm ? b.item_end[item] : b.cumsum[item];
+  const uint32_t ikey = b.ikeys[item];
+  const uint2 rc = b.rects[item];
+  float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  float cc = 0.f, smax = 0.f;
+  if (sp.tile_cull) {
+    r0 = b.records[(size_t)item * 3 + 0];
+    cc = b.records[(size_t)item * 3 + 1].x;
+    smax = b.records[(size_t)item * 3 + 2].y;
+  }
+  if (cnt == 0u) return;
   if (end > sp.icap || cnt > end) {
     atomicOr(&b.status->error, SKY_DEVERR_LISTS);
     return;
   }
-  const uint32_t dq = b.ikeys[item] & 0xFFFFu;  // depth16 (depth_key of the item's depth)
-  const uint2 rc = b.rects[item];
+  const uint32_t dq = ikey & 0xFFFFu;  // depth16 (depth_key of the item's depth)
   const uint32_t x0 = rc.x & 0xFFFFu, y0 = rc.x >> 16, x1 = rc.y & 0xFFFFu, y1 = rc.y >> 16;
   const uint32_t area = (x1 <= x0 || y1 <= y0) ? 0u : (x1 - x0) * (y1 - y0);
   uint32_t cur = end - cnt;
@@ -415,8 +431,6 @@ __global__ void __launch_bounds__(256) k_emit(DevBuffers b) {
   }
   // culled: the tiles the preprocess counted, by the same test on the same
   // record values
-  const float4 r0 = b.records[(size_t)item * 3 + 0];
-  const float cc = b.records[(size_t)item * 3 + 1].x, smax = b.records[(size_t)item * 3 + 2].y;
   EllipseRows e;
   if (!sp.tile_cull || !ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
     atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
@@ -1805,9 +1819,18 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   float prm[11];
 #pragma unroll
   for (int k = 0; k < 11; ++k) prm[k] = load_plane_rw(b.params, stride, k, g, r16);
-  for (int k = 0; k < 48; ++k) {
-    s_sh[k][t] = (!ref && k < 3 * ncoef) ? load_plane_rw(b.params, stride, 11 + k, g, r16) : 0.0f;
-    s_gsh[k][t] = 0.0f;
+  // 16 loads in flight at a time (a loop of load, then store, waits on each)
+#pragma unroll
+  for (int k0 = 0; k0 < 48; k0 += 16) {
+    float v[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+      v[j] = (!ref && k0 + j < 3 * ncoef) ? load_plane_rw(b.params, stride, 11 + k0 + j, g, r16) : 0.0f;
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      s_sh[k0 + j][t] = v[j];
+      s_gsh[k0 + j][t] = 0.0f;
+    }
   }
   Grad11 gr;
 #pragma unroll
