@@ -149,7 +149,7 @@ struct Context {
   // item order (view, depth16, Gaussian): sort keys, sorted keys, permutation
   Buf ikeys, ikeys_sorted, perm, item_end, isort_mem;
   SortScratch isort{};
-  Buf keys, keys_sorted, vals_sorted, rec_of, flatten, partials, tile_grads, gsum54;
+  Buf keys, keys_sorted, vals_sorted, rec_of, flatten, fmask, partials, tile_grads, gsum54;
   Buf offsets, loss_partials, color, alpha, tfinal, last, residual, targets, sort_mem;
   Buf flags, flag_scan, d_sp, d_st;
   // densification statistics (float4 per Gaussian) and multi-view scores
@@ -268,6 +268,7 @@ DevBuffers make_buffers(Context* c) {
   b.vals_sorted = (uint32_t*)c->vals_sorted.p;
   b.rec_of = (uint32_t*)c->rec_of.p;
   b.flatten = (uint32_t*)c->flatten.p;
+  b.fmask = (uint8_t*)c->fmask.p;
   b.partials = (float4*)c->partials.p;
   b.item_sums = (float4*)c->item_sums.p;
   b.tile_grads = (int32_t*)c->tile_grads.p;
@@ -304,6 +305,7 @@ int ensure_isect(Context* c, uint32_t need) {
   TRY(dev_alloc(c, c->vals_sorted, cap * 4));
   TRY(dev_alloc(c, c->rec_of, cap * 4));
   TRY(dev_alloc(c, c->flatten, cap * 4));
+  TRY(dev_alloc(c, c->fmask, cap));
   TRY(dev_alloc(c, c->partials, cap * kPartialF4 * 16));
   if (ref) TRY(dev_alloc(c, c->tile_grads, cap * 54 * 4));
   TRY(dev_alloc(c, c->sort_mem, sort_scratch_bytes((uint32_t)cap)));
@@ -1165,7 +1167,7 @@ int sky_destroy(void* p) {
   Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records, &c->aux,
                 &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->ikeys,
                 &c->ikeys_sorted, &c->perm, &c->item_end, &c->isort_mem, &c->keys,
-                &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->partials,
+                &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->fmask, &c->partials,
                 &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
                 &c->flag_scan, &c->d_sp, &c->d_st, &c->imp_stats, &c->dens_accum,

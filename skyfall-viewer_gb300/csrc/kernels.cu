@@ -719,7 +719,9 @@ __global__ void __launch_bounds__(TS* TS, TS == 16 ? 6 : 1) k_forward(DevBuffers
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
       stage_record(s_rec + k * 3, q0, q1, q2);
-      s_mask[k] = ellipse_band_mask<TS, 8, 4>(q0, q1, q2, tx * TS, ty * TS);
+      const uint32_t m = ellipse_band_mask<TS, 8, 4>(q0, q1, q2, tx * TS, ty * TS);
+      s_mask[k] = m;
+      if constexpr (TS == 16) b.fmask[bs + k] = (uint8_t)m;  // for the 16x16 backward
     }
     __syncthreads();
     // this warp's splats of the batch, in order (skipped splats cannot pass
@@ -1288,7 +1290,11 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float4 q0 = b.records[r * 3 + 0];
       const float4 q1 = b.records[r * 3 + 1];
       const float4 q2 = b.records[r * 3 + 2];
-      s_mask[k] = ellipse_band_mask<TS, 8, 8>(q0, q1, q2, tx * TS, ty * TS);
+      // the forward's 8x4-block ellipse mask of this intersection (it staged
+      // every intersection up to the tile's last contributor): an 8x8 block
+      // is kept when either of its two 8x4 halves is
+      const uint32_t m8 = b.fmask[bhi - k];
+      s_mask[k] = ((m8 | (m8 >> 2)) & 3u) | ((((m8 >> 4) | (m8 >> 6)) & 3u) << 2);
       // the box half-widths are only needed for the mask: the staged record
       // carries the splat's sure bound in their place
       stage_record(s_rec + k * 3, q0, q1, make_float4(q2.x, q2.y, sure_bound(q1, q2), q2.w));

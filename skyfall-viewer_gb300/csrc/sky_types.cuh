@@ -95,6 +95,8 @@ struct DevBuffers {
   uint32_t* vals_sorted;  // emission index per sorted intersection
   uint32_t* rec_of;       // item per emitted intersection
   uint32_t* flatten;      // item per sorted intersection
+  uint8_t* fmask;         // 16x16 tiles: per sorted intersection the forward staged, its
+                          // 8x4-block ellipse mask (bit 2 band + column)
   float4* partials;       // 3 float4 per intersection (emission order)
   float4* item_sums;      // exact mode: 3 float4 per item, its partials summed
   int32_t* tile_grads;    // reference mode: 54 per sorted intersection
