@@ -149,7 +149,7 @@ struct Context {
   // item order (view, depth16, Gaussian): sort keys, sorted keys, permutation
   Buf ikeys, ikeys_sorted, perm, item_end, isort_mem;
   SortScratch isort{};
-  Buf keys, keys_sorted, vals_sorted, rec_of, flatten, fmask, partials, tile_grads, gsum54;
+  Buf keys, keys_sorted, vals_sorted, rec_of, flatten, fmask, partials, reached, tile_grads, gsum54;
   Buf offsets, loss_partials, color, alpha, tfinal, last, residual, targets, sort_mem;
   Buf flags, flag_scan, d_sp, d_st;
   // densification statistics (float4 per Gaussian) and multi-view scores
@@ -269,6 +269,7 @@ DevBuffers make_buffers(Context* c) {
   b.rec_of = (uint32_t*)c->rec_of.p;
   b.flatten = (uint32_t*)c->flatten.p;
   b.fmask = (uint8_t*)c->fmask.p;
+  b.reached = (uint8_t*)c->reached.p;
   b.partials = (float4*)c->partials.p;
   b.item_sums = (float4*)c->item_sums.p;
   b.tile_grads = (int32_t*)c->tile_grads.p;
@@ -307,6 +308,8 @@ int ensure_isect(Context* c, uint32_t need) {
   TRY(dev_alloc(c, c->flatten, cap * 4));
   TRY(dev_alloc(c, c->fmask, cap));
   TRY(dev_alloc(c, c->partials, cap * kPartialF4 * 16));
+  TRY(dev_alloc(c, c->reached, cap));
+  CK(cudaMemsetAsync(c->reached.p, 0, c->reached.bytes, c->stream));
   if (ref) TRY(dev_alloc(c, c->tile_grads, cap * 54 * 4));
   TRY(dev_alloc(c, c->sort_mem, sort_scratch_bytes((uint32_t)cap)));
   c->sort = sort_scratch_carve(c->sort_mem.p, (uint32_t)cap);
@@ -411,6 +414,7 @@ int enqueue(Context* c, const Shape& sh, bool sizing_sync, uint64_t& launches, u
   TRY(mark(6));
   if (sh.mode >= kBackward) {
     if (sh.ref) CK(cudaMemsetAsync(c->gsum54.p, 0, items * 54 * 8, s));
+    else CK(cudaMemsetAsync(c->reached.p, 0, c->icap, s));  // the partials this step writes
     launch_backward(b, sh.max_tiles, c->cfg.tile_size, sh.bwd_batch, sh.ref, sh.count, s);
     TRY(mark(7));
     if (!sh.ref) {
@@ -1167,7 +1171,7 @@ int sky_destroy(void* p) {
   Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records, &c->aux,
                 &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->ikeys,
                 &c->ikeys_sorted, &c->perm, &c->item_end, &c->isort_mem, &c->keys,
-                &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->fmask, &c->partials,
+                &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->fmask, &c->partials, &c->reached,
                 &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,
                 &c->alpha, &c->tfinal, &c->last, &c->residual, &c->targets, &c->sort_mem, &c->flags,
                 &c->flag_scan, &c->d_sp, &c->d_st, &c->imp_stats, &c->dens_accum,
@@ -1732,6 +1736,11 @@ int sky_read_buffer(void* p, int which, void* dst, uint64_t bytes, uint64_t* siz
   if (!dst || sz == 0) return SKY_OK;
   if (bytes < sz) return fail(SKY_ERR_ARG, "destination holds %llu bytes, need %llu",
                               (unsigned long long)bytes, (unsigned long long)sz);
+  if (which == SKY_BUF_PARTIALS) {
+    // the exact backward writes only the partials it flags; the rest are zero
+    launch_partials_fill(make_buffers(c), (uint32_t)I, c->stream);
+    CK(cudaGetLastError());
+  }
   if (which == SKY_BUF_FLATTEN) {
     // the step resolved only the staged batches; complete it for the reader
     launch_flatten_fill(make_buffers(c), (uint32_t)I, c->stream);

@@ -934,6 +934,23 @@ SKY_DEV float warp_reduce_scatter9(const float v[9], uint32_t lane) {
   return z + __shfl_xor_sync(kFull, z, 1);
 }
 
+// The partial of sorted intersection i, at its emission index, flagged in
+// b.reached; one whose nine sums are all zero is not written (it counts as
+// zero, like the intersections no pixel reaches).
+SKY_DEV void write_partial(const DevBuffers& b, uint32_t i, const float sum[9], float dlogit, float dca,
+                           float dcb, float dcc, float dmx, float dmy) {
+  bool nz = false;
+#pragma unroll
+  for (int k = 0; k < 9; ++k) nz = nz || sum[k] != 0.0f;
+  if (!nz) return;
+  const uint32_t e = b.vals_sorted[i];
+  float4* dst = b.partials + (size_t)e * kPartialF4;
+  dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
+  dst[1] = make_float4(dca, dcb, dcc, dmx);
+  dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
+  b.reached[e] = 1u;
+}
+
 // Value index a lane holds after warp_reduce_scatter9, or 9 for none.
 SKY_DEV int scatter9_slot(uint32_t lane) {
   if (lane & 1u) return 9;
@@ -990,13 +1007,8 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
   const int slot = scatter9_slot(lane);
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
-  // intersections no pixel reaches get zero partials
-  for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
-    float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
-    dst[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-    dst[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    dst[2] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
+  // intersections beyond every pixel's last contributor are not written:
+  // their emission slots stay unflagged in b.reached and count as zero
   for (int bhi = hi; bhi >= (int)start; bhi -= kBwdBatch) {
     const int cnt = min(kBwdBatch, bhi - (int)start + 1);
     __syncthreads();
@@ -1106,10 +1118,7 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
       const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
       const float dmx = __fmaf_rn(q0.z, sum[7], q0.w * sum[8]);
       const float dmy = __fmaf_rn(q0.w, sum[7], q1.x * sum[8]);
-      float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
-      dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
-      dst[1] = make_float4(dca, dcb, dcc, dmx);
-      dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
+      write_partial(b, (uint32_t)i, sum, dlogit, dca, dcb, dcc, dmx, dmy);
     }
   }
 }
@@ -1275,13 +1284,8 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t n_eval = 0, n_contrib = 0, n_entries = 0, n_idle = 0;  // counting variant only
-  // intersections no pixel reaches get zero partials
-  for (int i = hi + 1 + (int)tid; i < (int)end; i += NT) {
-    float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
-    dst[0] = make_float4(0.f, 0.f, 0.f, 0.f);
-    dst[1] = make_float4(0.f, 0.f, 0.f, 0.f);
-    dst[2] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
+  // intersections beyond every pixel's last contributor are not written:
+  // their emission slots stay unflagged in b.reached and count as zero
   for (int bhi = hi; bhi >= (int)start; bhi -= kBatch) {
     const int cnt = min(kBatch, bhi - (int)start + 1);
     __syncthreads();
@@ -1364,10 +1368,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
       const float dmx = __fmaf_rn(ca, sum[7], q0.w * sum[8]);
       const float dmy = __fmaf_rn(q0.w, sum[7], cc * sum[8]);
-      float4* dst = b.partials + (size_t)b.vals_sorted[i] * kPartialF4;
-      dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
-      dst[1] = make_float4(dca, dcb, dcc, dmx);
-      dst[2] = make_float4(dmy, 0.0f, 0.0f, 0.0f);
+      write_partial(b, (uint32_t)i, sum, dlogit, dca, dcb, dcc, dmx, dmy);
     }
   }
   // (every lane walks the warp's list: lane 0's n_entries and n_idle are
@@ -1727,7 +1728,9 @@ constexpr int kGeomThreads = 128;
 // partials in emission order (pairs added as ((s + a) + c), an odd last one
 // alone), written as 3 float4.  A streaming pass with one thread per item,
 // so the geometry kernel reads one fixed-size record per view instead of a
-// variable-length chain of dependent loads.
+// variable-length chain of dependent loads.  Only partials the backward
+// flagged in b.reached are read; the others are zero (intersections beyond
+// every pixel's last contributor, about half of them, and all-zero sums).
 __global__ void __launch_bounds__(256) k_item_sums(DevBuffers b) {
   const StepParams& sp = *b.sp;
   if (capacity_failed(b.status)) return;
@@ -1741,20 +1744,22 @@ __global__ void __launch_bounds__(256) k_item_sums(DevBuffers b) {
     for (int k = 0; k < 9; ++k) in9[k] = 0.0f;
     const uint32_t e1 = b.perm ? b.item_end[item] : b.cumsum[item], e0 = e1 - cnt;
     uint32_t e = e0;
+    const float4 z = make_float4(0.f, 0.f, 0.f, 0.f);
     for (; e + 1 < e1; e += 2) {  // two partials in flight
-      const float4 a0 = b.partials[(size_t)e * 3 + 0];
-      const float4 a1 = b.partials[(size_t)e * 3 + 1];
-      const float4 a2 = b.partials[(size_t)e * 3 + 2];
-      const float4 c0 = b.partials[(size_t)e * 3 + 3];
-      const float4 c1 = b.partials[(size_t)e * 3 + 4];
-      const float4 c2 = b.partials[(size_t)e * 3 + 5];
+      const bool fa = b.reached[e] != 0u, fc = b.reached[e + 1] != 0u;
+      const float4 a0 = fa ? b.partials[(size_t)e * 3 + 0] : z;
+      const float4 a1 = fa ? b.partials[(size_t)e * 3 + 1] : z;
+      const float4 a2 = fa ? b.partials[(size_t)e * 3 + 2] : z;
+      const float4 c0 = fc ? b.partials[(size_t)e * 3 + 3] : z;
+      const float4 c1 = fc ? b.partials[(size_t)e * 3 + 4] : z;
+      const float4 c2 = fc ? b.partials[(size_t)e * 3 + 5] : z;
       in9[0] = (in9[0] + a0.x) + c0.x; in9[1] = (in9[1] + a0.y) + c0.y;
       in9[2] = (in9[2] + a0.z) + c0.z; in9[3] = (in9[3] + a0.w) + c0.w;
       in9[4] = (in9[4] + a1.x) + c1.x; in9[5] = (in9[5] + a1.y) + c1.y;
       in9[6] = (in9[6] + a1.z) + c1.z; in9[7] = (in9[7] + a1.w) + c1.w;
       in9[8] = (in9[8] + a2.x) + c2.x;
     }
-    if (e < e1) {
+    if (e < e1 && b.reached[e] != 0u) {
       const float4 a0 = b.partials[(size_t)e * 3 + 0];
       const float4 a1 = b.partials[(size_t)e * 3 + 1];
       const float4 a2 = b.partials[(size_t)e * 3 + 2];
@@ -2024,6 +2029,22 @@ void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s) {
     k_ranges<<<blocks, 256, 0, s>>>(b);
   }
   k_ranges_empty<<<1, 256, 0, s>>>(b);
+}
+
+// Zeroes the partials the last backward did not write (unflagged), for a
+// read-back of the buffer.
+__global__ void __launch_bounds__(256) k_partials_fill(DevBuffers b, uint32_t total) {
+  for (uint32_t e = blockIdx.x * blockDim.x + threadIdx.x; e < total; e += gridDim.x * blockDim.x)
+    if (b.reached[e] == 0u) {
+      float4* dst = b.partials + (size_t)e * kPartialF4;
+      dst[0] = dst[1] = dst[2] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+void launch_partials_fill(const DevBuffers& b, uint32_t total, cudaStream_t s) {
+  if (!total) return;
+  const uint32_t blocks = min((total + 255) / 256, (uint32_t)sm_count() * 16);
+  k_partials_fill<<<blocks, 256, 0, s>>>(b, total);
 }
 
 void launch_flatten_fill(const DevBuffers& b, uint32_t total, cudaStream_t s) {

@@ -12,6 +12,8 @@ uint32_t scan_block_count(uint32_t n_items);
 void launch_group_bounds(const DevBuffers& b, cudaStream_t s);
 void launch_emit(const DevBuffers& b, uint32_t n, uint32_t views, cudaStream_t s);
 void launch_ranges(const DevBuffers& b, uint32_t icap, cudaStream_t s);
+// Zeroes the partials the last exact backward left unwritten, for a read-back.
+void launch_partials_fill(const DevBuffers& b, uint32_t total, cudaStream_t s);
 // Completes flatten (the item of every sorted intersection) for a read-back.
 void launch_flatten_fill(const DevBuffers& b, uint32_t total, cudaStream_t s);
 // Splat-batch depths of the rasterizers: the forward stages fb splats per

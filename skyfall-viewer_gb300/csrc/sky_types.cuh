@@ -98,6 +98,7 @@ struct DevBuffers {
   uint8_t* fmask;         // 16x16 tiles: per sorted intersection the forward staged, its
                           // 8x4-block ellipse mask (bit 2 band + column)
   float4* partials;       // 3 float4 per intersection (emission order)
+  uint8_t* reached;       // per emission index: 1 when the exact backward wrote its partial
   float4* item_sums;      // exact mode: 3 float4 per item, its partials summed
   int32_t* tile_grads;    // reference mode: 54 per sorted intersection
   long long* gsum54;      // reference mode: 54 per item
