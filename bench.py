@@ -80,7 +80,7 @@ def parse():
     ap.add_argument("--fwd-batch", type=int, default=0, choices=[0, 64, 128, 256],
                     help="forward splat-batch depth (0 = 256)")
     ap.add_argument("--bwd-batch", type=int, default=0, choices=[0, 32, 64, 128],
-                    help="16x16-tile backward splat-batch depth (0 = 128)")
+                    help="16x16-tile backward splat-batch depth (0 = 64)")
     ap.add_argument("--tile-cull", type=int, default=1, choices=[0, 1],
                     help="1: intersection lists of the training steps hold only the tiles each "
                          "Gaussian's alpha >= 1/255 ellipse reaches (bit-identical results)")
@@ -805,7 +805,7 @@ def main():
             "workload": workload_name(args, n, B, C),
             "views_per_step": B, "global_batch": B, "parallelism": "replicas" if world > 1 else "none",
             "tile_size": args.tile_size, "fwd_batch": args.fwd_batch or 256,
-            "bwd_batch": (args.bwd_batch or 128) if args.tile_size == 16 else None,
+            "bwd_batch": (args.bwd_batch or 64) if args.tile_size == 16 else None,
             "tile_cull": bool(args.tile_cull),
             "autotune_ms_per_step": tune,
             "l2": "inputs > L2 (no flush)",

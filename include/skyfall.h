@@ -107,7 +107,7 @@ typedef struct SkyConfig {
   uint32_t fwd_batch;          /* splat-batch depth of the forward: 64, 128,
                                   256 (0 = 256)                              */
   uint32_t bwd_batch;          /* of the 16x16-tile exact backward: 32, 64,
-                                  128 (0 = 128); neither changes a result,
+                                  128 (0 = 64); neither changes a result,
                                   both may change with sky_set_config        */
   uint32_t tile_cull;          /* 1: the intersection lists of backward and
                                   training steps in the exact backward mode

@@ -332,12 +332,15 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint3
   __shared__ uint32_t s_warp[kScanThreads / 32];
   if (scan_skipped(b)) return;
   const uint32_t base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
-  uint32_t v[kScanItems];
+  uint32_t v[kScanItems], pi[kScanItems];
   uint32_t sum = 0;
 #pragma unroll
   for (int k = 0; k < kScanItems; ++k) {
     uint32_t i = base + k;
     v[k] = i < n_items ? scan_count(b, i) : 0u;
+    // the items of the scatter below, loaded ahead: a load after a store
+    // would wait for it (the arrays may alias as far as the compiler knows)
+    pi[k] = (b.perm && i < n_items) ? b.perm[i] : 0u;
     sum += v[k];
   }
   uint32_t total;
@@ -348,7 +351,7 @@ __global__ void __launch_bounds__(kScanThreads) k_scan_final(DevBuffers b, uint3
     uint32_t i = base + k;
     if (i < n_items) {
       b.cumsum[i] = run;
-      if (b.perm) b.item_end[b.perm[i]] = run;
+      if (b.perm) b.item_end[pi[k]] = run;
     }
   }
 }
@@ -1706,20 +1709,61 @@ SKY_DEV void geom_cov_final(const float* prm /*11 geometry params*/, const float
   for (int k = 0; k < 3; ++k) gr.ls[k] += dsig[k] * sig[k] * lsg[k];
 }
 
-SKY_DEV void adam_elem(float* __restrict__ p, float* __restrict__ m1, float* __restrict__ m2,
-                       size_t idx, float g, float lr, const StepParams& sp) {
-  const float pm1 = m1[idx], pm2 = m2[idx];
-  const float a = sp.beta1 * pm1;
-  const float bb = (1.0f - sp.beta1) * g;
+// The step's Adam constants (adam.wgsl's uniforms), read once.
+struct AdamK {
+  float b1, omb1, b2, omb2, eps, bc1_rcp, bc2_sqrt_rcp;
+};
+SKY_DEV AdamK adam_consts(const StepParams& sp) {
+  return AdamK{sp.beta1, 1.0f - sp.beta1, sp.beta2, 1.0f - sp.beta2, sp.adam_eps, sp.bc1_rcp,
+               sp.bc2_sqrt_rcp};
+}
+
+// One Adam update of a parameter p and its moments m1, m2 (values, updated in
+// place), in the reference's operation order.
+SKY_DEV void adam_vals(float& p, float& m1, float& m2, float g, float lr, const AdamK& k) {
+  const float a = k.b1 * m1;
+  const float bb = k.omb1 * g;
   const float nm1 = a + bb;
-  const float c = sp.beta2 * pm2;
-  const float d = ((1.0f - sp.beta2) * g) * g;
+  const float c = k.b2 * m2;
+  const float d = (k.omb2 * g) * g;
   const float nm2 = c + d;
-  const float denom = sqrtf(nm2) * sp.bc2_sqrt_rcp + sp.adam_eps;
-  const float step = lr * sp.bc1_rcp;
-  p[idx] = p[idx] - step * (nm1 / denom);
-  m1[idx] = nm1;
-  m2[idx] = nm2;
+  const float denom = sqrtf(nm2) * k.bc2_sqrt_rcp + k.eps;
+  const float step = lr * k.bc1_rcp;
+  p = p - step * (nm1 / denom);
+  m1 = nm1;
+  m2 = nm2;
+}
+
+// N values passed by value (an array captured by reference would be placed
+// in local memory).
+template <int N>
+struct Vals {
+  float v[N];
+};
+
+// Adam over N consecutive planes of Gaussian g: every load first, then the
+// updates, then the stores (a load after a store to another plane would wait
+// for it: the arrays may alias as far as the compiler knows).
+template <int N>
+SKY_DEV void adam_planes(const DevBuffers& b, uint32_t stride, int plane0, uint32_t g, Vals<N> grad,
+                         Vals<N> lr, const AdamK& k) {
+  float P[N], M1[N], M2[N];
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    const size_t idx = (size_t)(plane0 + j) * stride + g;
+    P[j] = b.params[idx];
+    M1[j] = b.m1[idx];
+    M2[j] = b.m2[idx];
+  }
+#pragma unroll
+  for (int j = 0; j < N; ++j) adam_vals(P[j], M1[j], M2[j], grad.v[j], lr.v[j], k);
+#pragma unroll
+  for (int j = 0; j < N; ++j) {
+    const size_t idx = (size_t)(plane0 + j) * stride + g;
+    b.params[idx] = P[j];
+    b.m1[idx] = M1[j];
+    b.m2[idx] = M2[j];
+  }
 }
 
 constexpr int kGeomThreads = 128;
@@ -1983,14 +2027,20 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     for (int k = 0; k < 48; ++k) b.grads[(size_t)(11 + k) * stride + g] = s_gsh[k][t];
   }
   if (sp.apply_adam) {
-#pragma unroll
-    for (int k = 0; k < 11; ++k) {
-      const float lr = k < 3 ? sp.lr_pos : (k < 6 ? sp.lr_scale : (k < 10 ? sp.lr_rot : sp.lr_opacity));
-      adam_elem(b.params, b.m1, b.m2, (size_t)k * stride + g, g11[k], lr, sp);
-    }
+    const AdamK ak = adam_consts(sp);
+    const float lr_pos = sp.lr_pos, lr_scale = sp.lr_scale, lr_rot = sp.lr_rot, lr_op = sp.lr_opacity;
+    const float lr_sh = sp.lr_sh;
+    adam_planes<6>(b, stride, 0, g, Vals<6>{{g11[0], g11[1], g11[2], g11[3], g11[4], g11[5]}},
+                   Vals<6>{{lr_pos, lr_pos, lr_pos, lr_scale, lr_scale, lr_scale}}, ak);
+    adam_planes<5>(b, stride, 6, g, Vals<5>{{g11[6], g11[7], g11[8], g11[9], g11[10]}},
+                   Vals<5>{{lr_rot, lr_rot, lr_rot, lr_rot, lr_op}}, ak);
     if (sp.sh_update) {
-      for (int k = 0; k < 48; ++k)
-        adam_elem(b.params, b.m1, b.m2, (size_t)(11 + k) * stride + g, s_gsh[k][t], sp.lr_sh, sp);
+#pragma unroll
+      for (int k0 = 0; k0 < 48; k0 += 8)
+        adam_planes<8>(b, stride, 11 + k0, g,
+                       Vals<8>{{s_gsh[k0][t], s_gsh[k0 + 1][t], s_gsh[k0 + 2][t], s_gsh[k0 + 3][t],
+                                s_gsh[k0 + 4][t], s_gsh[k0 + 5][t], s_gsh[k0 + 6][t], s_gsh[k0 + 7][t]}},
+                       Vals<8>{{lr_sh, lr_sh, lr_sh, lr_sh, lr_sh, lr_sh, lr_sh, lr_sh}}, ak);
     }
   }
 }
@@ -2097,7 +2147,7 @@ void launch_backward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint3
         }
         switch (bb) {
           case 32: k_backward_exact2<32><<<max_tiles, 128, 0, s>>>(b); break;
-          case 64: k_backward_exact2<64><<<max_tiles, 128, 0, s>>>(b); break;
+          case 128: k_backward_exact2<128><<<max_tiles, 128, 0, s>>>(b); break;
           default: k_backward_exact2<kBwdBatch16><<<max_tiles, 128, 0, s>>>(b); break;
         }
         break;

@@ -19,7 +19,7 @@ void launch_flatten_fill(const DevBuffers& b, uint32_t total, cudaStream_t s);
 // Splat-batch depths of the rasterizers: the forward stages fb splats per
 // batch (64, 128 or 256), the 16x16-tile exact backward bb (32, 64 or 128);
 // other values select the defaults.  Results do not depend on them.
-constexpr uint32_t kBwdBatch16 = 128;  // default backward depth for 16x16 tiles
+constexpr uint32_t kBwdBatch16 = 64;  // default backward depth for 16x16 tiles
 // count: the pair-counting variants (16x16 tiles at the default depths
 // only; other shapes launch the plain kernels and count nothing).
 void launch_forward(const DevBuffers& b, uint32_t max_tiles, uint32_t ts, uint32_t fb, bool ssim,
