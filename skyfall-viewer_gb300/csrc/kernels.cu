@@ -1232,6 +1232,57 @@ SKY_DEV void lane_moments(float val[9], float dx) {
   val[8] = gy;
 }
 
+// The warp's nine moment sums of an entry from the lanes' raw sums (bwd_pair's
+// val[0..6]), column first: the four lanes of a pixel column (lane & 7) share
+// dx, so the seven raw sums are added over the column (lanes l ^ 8, l ^ 16)
+// before the g sums are expanded by dx, and only then over the eight columns
+// (10 shuffles instead of 12, and the expansion once per column).  After the
+// column step a lane of row group (lane >> 3) & 3 holds two sums u0, u1
+// ({c0, c1}, {c2, g}, {o, g dy}, {g dy^2, -}) and forms u0, u1 f1, u1 f2 from
+// its factors f1 = a1 + dx (b1 + dx c1), f2 = a2 + dx b2.  On return the lane
+// with cols9_slot(lane) == k < 9 holds the warp total of lane_moments' k-th
+// value.
+struct ColFactors {
+  float a1, b1, c1, a2, b2;
+};
+SKY_DEV ColFactors col_factors(uint32_t lane) {
+  switch ((lane >> 3) & 3u) {
+    case 0: return {1.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // c1 (x1), -
+    case 1: return {0.0f, 0.0f, 1.0f, 0.0f, 1.0f};  // g dx^2, g dx
+    case 2: return {0.0f, 1.0f, 0.0f, 1.0f, 0.0f};  // g dy dx, g dy
+    default: return {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  }
+}
+SKY_DEV int cols9_slot(uint32_t lane) {
+  if (lane & 1u) return 9;
+  const int xi = (int)((lane >> 2) & 1u) * 2 + (int)((lane >> 1) & 1u);
+  switch ((lane >> 3) & 3u) {
+    case 0: return xi == 0 ? 0 : (xi == 1 ? 1 : 9);
+    case 1: return xi == 0 ? 2 : (xi == 1 ? 4 : (xi == 2 ? 7 : 9));
+    case 2: return xi == 0 ? 3 : (xi == 1 ? 5 : (xi == 2 ? 8 : 9));
+    default: return xi == 0 ? 6 : 9;
+  }
+}
+SKY_DEV float warp_reduce_cols9(const float val[9], float dx, uint32_t lane, const ColFactors& f) {
+  const bool b4 = lane & 16u, b3 = lane & 8u, b2 = lane & 4u, b1 = lane & 2u;
+  const float v[8] = {val[0], val[1], val[2], val[4], val[3], val[5], val[6], 0.0f};
+  float w[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    w[i] = (b4 ? v[i + 4] : v[i]) + __shfl_xor_sync(kFull, b4 ? v[i] : v[i + 4], 16);
+  float u[2];
+#pragma unroll
+  for (int i = 0; i < 2; ++i)
+    u[i] = (b3 ? w[i + 2] : w[i]) + __shfl_xor_sync(kFull, b3 ? w[i] : w[i + 2], 8);
+  const float f1 = __fmaf_rn(dx, __fmaf_rn(dx, f.c1, f.b1), f.a1);
+  const float f2 = __fmaf_rn(dx, f.b2, f.a2);
+  const float x0 = u[0], x1 = u[1] * f1, x2 = u[1] * f2;
+  const float y0 = (b2 ? x2 : x0) + __shfl_xor_sync(kFull, b2 ? x0 : x2, 4);
+  const float y1 = (b2 ? 0.0f : x1) + __shfl_xor_sync(kFull, b2 ? x1 : 0.0f, 4);
+  const float z = (b1 ? y1 : y0) + __shfl_xor_sync(kFull, b1 ? y0 : y1, 2);
+  return z + __shfl_xor_sync(kFull, z, 1);
+}
+
 // BB: the splat-batch depth (32, 64 or 128 staged splats); the per-splat sums
 // do not depend on it.
 template <int BB, bool CNT = false>
@@ -1283,7 +1334,8 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   __syncthreads();
   int hi = s_hi[0];
   for (int w = 1; w < NW; ++w) hi = max(hi, s_hi[w]);
-  const int slot = scatter9_slot(lane);
+  const int slot = cols9_slot(lane);
+  const ColFactors cf = col_factors(lane);
   const uint32_t wbit = 1u << warp;
   const uint32_t lt = (1u << lane) - 1u;
   uint32_t n_eval = 0, n_contrib = 0, n_entries = 0, n_idle = 0;  // counting variant only
@@ -1338,18 +1390,18 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
         if (i <= pix[0].hi) contrib = bwd_pair(pix[0], dx, s1, bdx, q0, q1, q2, s_sure, val);
         if (i <= pix[1].hi) contrib = bwd_pair(pix[1], dx, s1, bdx, q0, q1, q2, s_sure, val) || contrib;
       }
-      lane_moments(val, dx);
       const uint32_t who = __ballot_sync(kFull, contrib);
       if constexpr (CNT) n_idle += who == 0u ? 1u : 0u;
       if (who == 0u) {
         if (slot < 9) s_part[warp][j][slot] = 0.0f;
       } else if ((who & (who - 1u)) == 0u) {
         if (contrib) {
+          lane_moments(val, dx);
 #pragma unroll
           for (int k = 0; k < 9; ++k) s_part[warp][j][k] = val[k];
         }
       } else {
-        const float tot = warp_reduce_scatter9(val, lane);
+        const float tot = warp_reduce_cols9(val, dx, lane, cf);
         if (slot < 9) s_part[warp][j][slot] = tot;
       }
     }
