@@ -79,3 +79,28 @@ def test_graph_regrows_capacity(sky):
     assert np.array_equal(out[0][1], out[1][1])
     assert out[0][2] == 0 and out[1][2] >= 3   # steps 2.. replayed a graph
     assert out[1][3] >= 2                      # and it was re-captured after growing
+
+
+def test_counting_variants_match_plain_kernels(sky):
+    """Profiling level 2 runs the raster kernels' counting variants, which
+    tally evaluated and contributing pairs and list entries; level 0 runs
+    the plain ones.  Both must train bit for bit alike, with culled lists and
+    with full ones, on the graph path and on direct launches."""
+    P = scenes.scene_clusters(30000, seed=57, clusters=8, center_range=1.0, logscale_mean=-4.0)
+    cams = scenes.cameras_mixed(4, 4.0, seed=58)
+    cams = [dict(c, width=c["width"] // 2, height=c["height"] // 2,
+                 focal=c["focal"] / 2, proj=c["proj"]) for c in cams]
+    tgt = [scenes.target_uniform(c["width"], c["height"], seed=90 + k) for k, c in enumerate(cams)]
+    plan = [[0, 1, 2, 3], [3, 1], [2, 0, 1], [1, 2, 3, 0]]
+    for graph, cull in ((True, True), (False, False)):
+        out = []
+        for level in (0, 2):
+            r = trainer(sky, P, cams, tgt, graph)
+            r.setTileCull(cull)
+            r.enableProfiling(level)
+            losses = [r.trainStep(v).loss for v in plan]
+            out.append((losses, r.params(), r.moments()))
+            r.close()
+        assert out[0][0] == out[1][0]
+        assert np.array_equal(out[0][1], out[1][1])
+        assert np.array_equal(out[0][2][0], out[1][2][0]) and np.array_equal(out[0][2][1], out[1][2][1])
