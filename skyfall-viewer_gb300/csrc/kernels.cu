@@ -23,6 +23,24 @@ SKY_DEV float load_plane_rw(const float* P, uint32_t stride, int plane, uint32_t
   return r16 ? round_f16(v) : v;
 }
 
+// Asynchronous global -> shared copies (16 bytes through L2; 8 and 4 through
+// L1), and their group fences.
+SKY_DEV void cp_async16(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+SKY_DEV void cp_async8(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+SKY_DEV void cp_async4(void* smem, const void* gmem) {
+  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+SKY_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+SKY_DEV void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+SKY_DEV void cp_async_wait0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 SKY_DEV int find_view(const StepParams& sp, uint32_t tile) {
   int v = 0;
   for (int k = 1; k < (int)sp.num_views; ++k)
@@ -233,17 +251,23 @@ __global__ void __launch_bounds__(kPrepThreads, 8) k_preprocess(DevBuffers b) {
   const uint32_t stride = sp.plane_stride;
   const int deg = (int)sp.sh_deg;
   const int nsh = 3 * (deg + 1) * (deg + 1);
+  // the SH coefficients go to this thread's column of s_sh by asynchronous
+  // copies, all in flight at once and holding no registers (loads into
+  // registers would have to be stored in groups of a few), then rounded in
+  // place
+#pragma unroll
+  for (int k = 0; k < 48; ++k) {
+    if (k < nsh) cp_async4(&s_sh[k][t], &b.params[(size_t)(11 + k) * stride + g]);
+    else s_sh[k][t] = 0.0f;
+  }
+  cp_async_commit();
   float prm[11];
 #pragma unroll
   for (int k = 0; k < 11; ++k) prm[k] = load_plane(b.params, stride, k, g, r16);
-  // 4 loads in flight at a time (a loop of load, then store, waits on each)
+  cp_async_wait0();
+  if (r16) {
 #pragma unroll
-  for (int k0 = 0; k0 < 48; k0 += 4) {
-    float v[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) v[j] = k0 + j < nsh ? load_plane(b.params, stride, 11 + k0 + j, g, r16) : 0.0f;
-#pragma unroll
-    for (int j = 0; j < 4; ++j) s_sh[k0 + j][t] = v[j];
+    for (int k = 0; k < 48; ++k) s_sh[k][t] = round_f16(s_sh[k][t]);
   }
   auto get = [&](int plane) { return plane < 11 ? prm[plane] : s_sh[plane - 11][t]; };
   // the covariance, opacity and skip bound do not depend on the view
@@ -1870,18 +1894,6 @@ __global__ void __launch_bounds__(256) k_item_sums(DevBuffers b) {
   }
 }
 
-// Asynchronous 16-byte global -> shared copy through L2, and its group fences.
-SKY_DEV void cp_async16(void* smem, const void* gmem) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-SKY_DEV void cp_async8(void* smem, const void* gmem) {
-  const uint32_t s = (uint32_t)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(s), "l"(gmem) : "memory");
-}
-SKY_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
-SKY_DEV void cp_async_wait1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
-
 // Dynamic shared memory of k_geom_adam: SH values and SH-gradient
 // accumulators (48 x threads f32 each), two buffers of the threads' item
 // sums (3 float4 per thread) and two of their (depth, radius) pairs.
@@ -1923,21 +1935,22 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
   const int ncoef = (deg + 1) * (deg + 1);
   const bool ref = sp.bwd_mode != 0;
   const bool need_sh_grads = sp.sh_update || sp.write_grads;
+  // the SH coefficients go to this thread's column of s_sh by asynchronous
+  // copies, all in flight at once, then rounded in place
+#pragma unroll
+  for (int k = 0; k < 48; ++k) {
+    if (!ref && k < 3 * ncoef) cp_async4(&s_sh[k][t], &b.params[(size_t)(11 + k) * stride + g]);
+    else s_sh[k][t] = 0.0f;
+    s_gsh[k][t] = 0.0f;
+  }
+  cp_async_commit();
   float prm[11];
 #pragma unroll
   for (int k = 0; k < 11; ++k) prm[k] = load_plane_rw(b.params, stride, k, g, r16);
-  // 16 loads in flight at a time (a loop of load, then store, waits on each)
+  cp_async_wait0();
+  if (r16) {
 #pragma unroll
-  for (int k0 = 0; k0 < 48; k0 += 16) {
-    float v[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j)
-      v[j] = (!ref && k0 + j < 3 * ncoef) ? load_plane_rw(b.params, stride, 11 + k0 + j, g, r16) : 0.0f;
-#pragma unroll
-    for (int j = 0; j < 16; ++j) {
-      s_sh[k0 + j][t] = v[j];
-      s_gsh[k0 + j][t] = 0.0f;
-    }
+    for (int k = 0; k < 48; ++k) s_sh[k][t] = round_f16(s_sh[k][t]);
   }
   Grad11 gr;
 #pragma unroll
