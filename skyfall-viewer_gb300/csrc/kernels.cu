@@ -2095,17 +2095,19 @@ __global__ void __launch_bounds__(kGeomThreads, 3) k_geom_adam(DevBuffers b) {
     const AdamK ak = adam_consts(sp);
     const float lr_pos = sp.lr_pos, lr_scale = sp.lr_scale, lr_rot = sp.lr_rot, lr_op = sp.lr_opacity;
     const float lr_sh = sp.lr_sh;
-    adam_planes<6>(b, stride, 0, g, Vals<6>{{g11[0], g11[1], g11[2], g11[3], g11[4], g11[5]}},
-                   Vals<6>{{lr_pos, lr_pos, lr_pos, lr_scale, lr_scale, lr_scale}}, ak);
-    adam_planes<5>(b, stride, 6, g, Vals<5>{{g11[6], g11[7], g11[8], g11[9], g11[10]}},
-                   Vals<5>{{lr_rot, lr_rot, lr_rot, lr_rot, lr_op}}, ak);
+    adam_planes<11>(b, stride, 0, g,
+                    Vals<11>{{g11[0], g11[1], g11[2], g11[3], g11[4], g11[5], g11[6], g11[7], g11[8],
+                              g11[9], g11[10]}},
+                    Vals<11>{{lr_pos, lr_pos, lr_pos, lr_scale, lr_scale, lr_scale, lr_rot, lr_rot,
+                              lr_rot, lr_rot, lr_op}}, ak);
     if (sp.sh_update) {
 #pragma unroll
-      for (int k0 = 0; k0 < 48; k0 += 8)
-        adam_planes<8>(b, stride, 11 + k0, g,
-                       Vals<8>{{s_gsh[k0][t], s_gsh[k0 + 1][t], s_gsh[k0 + 2][t], s_gsh[k0 + 3][t],
-                                s_gsh[k0 + 4][t], s_gsh[k0 + 5][t], s_gsh[k0 + 6][t], s_gsh[k0 + 7][t]}},
-                       Vals<8>{{lr_sh, lr_sh, lr_sh, lr_sh, lr_sh, lr_sh, lr_sh, lr_sh}}, ak);
+      for (int k0 = 0; k0 < 48; k0 += 12) {
+        Vals<12> gv, lv;
+#pragma unroll
+        for (int j = 0; j < 12; ++j) { gv.v[j] = s_gsh[k0 + j][t]; lv.v[j] = lr_sh; }
+        adam_planes<12>(b, stride, 11 + k0, g, gv, lv, ak);
+      }
     }
   }
 }
