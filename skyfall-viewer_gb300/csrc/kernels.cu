@@ -710,6 +710,7 @@ __global__ void __launch_bounds__(TS* TS, TS == 16 ? 6 : 1) k_forward(DevBuffers
   __shared__ uint32_t s_mask[FB];
   __shared__ uint8_t s_list[NW][FB];
   __shared__ double s_loss[NW];
+  __shared__ float4 s_tgt[NT];  // this thread's target pixel, copied in during the loop
   const StepParams& sp = *b.sp;
   const uint32_t tile = blockIdx.x;
   if (tile >= sp.num_tiles) return;
@@ -726,6 +727,9 @@ __global__ void __launch_bounds__(TS* TS, TS == 16 ? 6 : 1) k_forward(DevBuffers
   const bool inside = x < vi.width && y < vi.height;
   const uint32_t start = b.offsets[tile], end = b.offsets[tile + 1];
   const float pxf = (float)x + 0.5f, pyf = (float)y + 0.5f;
+  const bool want_tgt = inside && sp.has_loss && vi.has_target;
+  if (want_tgt) cp_async16(&s_tgt[tid], &b.targets[(size_t)vi.target_base + (size_t)y * vi.width + x]);
+  cp_async_commit();
   float C0 = 0.0f, C1 = 0.0f, C2 = 0.0f, A = 0.0f, Tp = 1.0f;
   // the reference's loop visits every intersection of the tile up to the
   // one that ends it (training-forward-tiles.wgsl:168-207)
@@ -810,8 +814,9 @@ __global__ void __launch_bounds__(TS* TS, TS == 16 ? 6 : 1) k_forward(DevBuffers
     b.alpha[p] = A;
     b.tfinal[p] = Tp;
     b.last[p] = last;
-    if (sp.has_loss && vi.has_target) {
-      const float4 tg = b.targets[(size_t)vi.target_base + (size_t)y * vi.width + x];
+    cp_async_wait0();
+    if (want_tgt) {
+      const float4 tg = s_tgt[tid];
       const float d0 = o0 - tg.x, d1 = o1 - tg.y, d2 = o2 - tg.z;
       auto sgn = [](float d) { return d > 0.0f ? 1.0f : (d < 0.0f ? -1.0f : 0.0f); };
       const float g0 = sp.w_l2 * d0 + sp.w_l1 * sgn(d0);
