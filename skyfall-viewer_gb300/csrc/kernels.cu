@@ -934,10 +934,10 @@ __global__ void __launch_bounds__(1024) k_loss_final(DevBuffers b) {
 // Gaussian later).  A warp skips a splat whose alpha >= 1/255 box misses all
 // of its pixels or that lies beyond all of its pixels' last contributors.
 // Each batch's per-pair values are reduced over the warp by a fixed
-// reduce-scatter (12 shuffles for 9 values), then over the warps in index
-// order, and written per intersection to partials[emission index] -- so
-// every Gaussian's partials are contiguous and the later per-Gaussian sum
-// has a fixed order.
+// reduce-scatter (12 shuffles for 9 values; column first, 10 shuffles, in
+// the 16x16 kernel), then over the warps in index order, and written per
+// intersection to partials[emission index] -- so every Gaussian's partials
+// are contiguous and the later per-Gaussian sum has a fixed order.
 // ---------------------------------------------------------------------------
 
 // Sum of v[0..8] over the warp, scattered: on return the lane with bit 0
