@@ -911,8 +911,20 @@ __global__ void __launch_bounds__(1024) k_loss_final(DevBuffers b) {
   __shared__ double s[32];
   const StepParams& sp = *b.sp;
   double acc = 0.0;
-  // fixed assignment of tiles to threads, then a fixed tree
-  for (uint32_t t = threadIdx.x; t < sp.num_tiles; t += blockDim.x) acc += b.loss_partials[t];
+  // fixed assignment of tiles to threads, then a fixed tree; a thread's
+  // partials are loaded 16 at a time and added in order (one load, one add
+  // after another would wait on every load)
+  constexpr uint32_t kAhead = 16;
+  const uint32_t nt = sp.num_tiles, step = blockDim.x;
+  uint32_t t = threadIdx.x;
+  for (; t + (kAhead - 1) * step < nt; t += kAhead * step) {
+    double v[kAhead];
+#pragma unroll
+    for (uint32_t k = 0; k < kAhead; ++k) v[k] = b.loss_partials[t + k * step];
+#pragma unroll
+    for (uint32_t k = 0; k < kAhead; ++k) acc += v[k];
+  }
+  for (; t < nt; t += step) acc += b.loss_partials[t];
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
   if ((threadIdx.x & 31) == 0) s[threadIdx.x >> 5] = acc;
