@@ -978,16 +978,15 @@ SKY_DEV float warp_reduce_scatter9(const float v[9], uint32_t lane) {
   return z + __shfl_xor_sync(kFull, z, 1);
 }
 
-// The partial of sorted intersection i, at its emission index, flagged in
+// The partial of a sorted intersection, at its emission index e, flagged in
 // b.reached; one whose nine sums are all zero is not written (it counts as
 // zero, like the intersections no pixel reaches).
-SKY_DEV void write_partial(const DevBuffers& b, uint32_t i, const float sum[9], float dlogit, float dca,
+SKY_DEV void write_partial(const DevBuffers& b, uint32_t e, const float sum[9], float dlogit, float dca,
                            float dcb, float dcc, float dmx, float dmy) {
   bool nz = false;
 #pragma unroll
   for (int k = 0; k < 9; ++k) nz = nz || sum[k] != 0.0f;
   if (!nz) return;
-  const uint32_t e = b.vals_sorted[i];
   float4* dst = b.partials + (size_t)e * kPartialF4;
   dst[0] = make_float4(sum[0], sum[1], sum[2], dlogit);
   dst[1] = make_float4(dca, dcb, dcc, dmx);
@@ -1162,7 +1161,7 @@ __global__ void __launch_bounds__(TS* TS) k_backward_exact(DevBuffers b) {
       const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
       const float dmx = __fmaf_rn(q0.z, sum[7], q0.w * sum[8]);
       const float dmy = __fmaf_rn(q0.w, sum[7], q1.x * sum[8]);
-      write_partial(b, (uint32_t)i, sum, dlogit, dca, dcb, dcc, dmx, dmy);
+      write_partial(b, b.vals_sorted[i], sum, dlogit, dca, dcb, dcc, dmx, dmy);
     }
   }
 }
@@ -1328,8 +1327,8 @@ SKY_DEV float warp_reduce_cols9(const float val[9], float dx, uint32_t lane, con
 // do not depend on it.
 template <int BB, bool CNT = false>
 __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
-  static_assert(BB <= 256, "list entries are bytes");
   constexpr int TS = 16, NT = 128, NW = 4, kBatch = BB;
+  static_assert(BB <= NT, "one staged splat per thread and batch");
   __shared__ float4 s_rec[kBatch * 3];
   __shared__ uint32_t s_mask[kBatch];
   __shared__ float s_part[NW][kBatch][9];
@@ -1385,7 +1384,11 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
   for (int bhi = hi; bhi >= (int)start; bhi -= kBatch) {
     const int cnt = min(kBatch, bhi - (int)start + 1);
     __syncthreads();
+    // thread k stages splat k and later writes its partial: its emission
+    // index is loaded here, off the write's path
+    uint32_t e_mine = 0;
     for (int k = (int)tid; k < cnt; k += NT) {
+      e_mine = b.vals_sorted[bhi - k];
       const size_t r = b.flatten[bhi - k];
       const float4 q0 = b.records[r * 3 + 0];
       const float4 q1 = b.records[r * 3 + 1];
@@ -1447,7 +1450,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       }
     }
     __syncthreads();
-    for (int j = (int)tid; j < cnt; j += NT) {
+    for (int j = (int)tid; j < cnt; j += NT) {  // (j = tid: the thread that staged it)
       const int i = bhi - j;
       const uint32_t m = s_mask[j];
       float sum[9];
@@ -1464,7 +1467,7 @@ __global__ void __launch_bounds__(128, 8) k_backward_exact2(DevBuffers b) {
       const float dca = -0.5f * sum[4], dcb = -sum[5], dcc = -0.5f * sum[6];
       const float dmx = __fmaf_rn(ca, sum[7], q0.w * sum[8]);
       const float dmy = __fmaf_rn(q0.w, sum[7], cc * sum[8]);
-      write_partial(b, (uint32_t)i, sum, dlogit, dca, dcb, dcc, dmx, dmy);
+      write_partial(b, e_mine, sum, dlogit, dca, dcb, dcc, dmx, dmy);
     }
   }
   // (every lane walks the warp's list: lane 0's n_entries and n_idle are
