@@ -145,7 +145,7 @@ struct Context {
   cudaStream_t stream = nullptr;
   uint32_t n = 0, stride = 0;
   Buf params, m1, m2, grads, tmp_planes;
-  Buf records, aux, counts, rects, cumsum, block_sums;
+  Buf records, aux, counts, rects, rowspans, cumsum, block_sums;
   // item order (view, depth16, Gaussian): sort keys, sorted keys, permutation
   Buf ikeys, ikeys_sorted, perm, item_end, isort_mem;
   SortScratch isort{};
@@ -257,6 +257,7 @@ DevBuffers make_buffers(Context* c) {
   b.aux = (float2*)c->aux.p;
   b.counts = (uint32_t*)c->counts.p;
   b.rects = (uint2*)c->rects.p;
+  b.rowspans = (uint4*)c->rowspans.p;
   b.ikeys = (uint32_t*)c->ikeys.p;
   b.perm = (uint32_t*)c->perm.p;
   b.ikeys_sorted = (uint32_t*)c->ikeys_sorted.p;
@@ -519,6 +520,7 @@ int run_views(Context* c, const uint32_t* cams, uint32_t nv, Mode mode, SkyStepS
   TRY(dev_alloc(c, c->aux, items * 8));
   TRY(dev_alloc(c, c->counts, items * 4));
   TRY(dev_alloc(c, c->rects, items * 8));
+  TRY(dev_alloc(c, c->rowspans, items * 16));
   TRY(dev_alloc(c, c->cumsum, items * 4));
   TRY(dev_alloc(c, c->ikeys, items * 4));
   TRY(dev_alloc(c, c->ikeys_sorted, items * 4));
@@ -1169,7 +1171,7 @@ int sky_destroy(void* p) {
   if (!c) return SKY_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
   Buf* all[] = {&c->params, &c->m1, &c->m2, &c->grads, &c->tmp_planes, &c->records, &c->aux,
-                &c->counts, &c->rects, &c->cumsum, &c->block_sums, &c->ikeys,
+                &c->counts, &c->rects, &c->rowspans, &c->cumsum, &c->block_sums, &c->ikeys,
                 &c->ikeys_sorted, &c->perm, &c->item_end, &c->isort_mem, &c->keys,
                 &c->keys_sorted, &c->vals_sorted, &c->rec_of, &c->flatten, &c->fmask, &c->partials, &c->reached,
                 &c->tile_grads, &c->gsum54, &c->offsets, &c->loss_partials, &c->color,

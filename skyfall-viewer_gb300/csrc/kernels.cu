@@ -81,6 +81,11 @@ SKY_DEV uint32_t rect_area(uint2 rc) {
 // evaluation of s is within 3e-4 s of the exact value at their f32 offsets
 // (dx, dy): every pixel that passes the pre-filter has those offsets inside E.
 // Worse-conditioned conics (and smax <= 0) get no EllipseRows.
+// Culled lists: an item whose rectangle has at most kSpanRows tile rows and
+// at most 255 tile columns keeps its rows' spans (as the preprocess counted
+// them) for the key emission, two bytes per row.
+constexpr uint32_t kSpanRows = 8;
+
 struct EllipseRows {
   float mx, my, a, b, det, two_a_l;
   float V, v_margin;  // V, and 1.01 V + 0.05: the rows listed
@@ -209,8 +214,24 @@ SKY_DEV void write_projection(const DevBuffers& b, const ProjOut& o, bool ok, fl
       count = 0u;
     } else if (ellipse_rows(o.mx, o.my, o.ca, o.cb, o.cc, smax, e)) {
       count = 0u;
-      uint32_t lo;
-      for (uint32_t ty = o.y0; ty < o.y1; ++ty) count += row_span(e, ty, o.x0, o.x1, sp.tile_size, lo);
+      const bool keep = o.y1 - o.y0 <= kSpanRows && o.x1 - o.x0 <= 255u;
+      uint32_t w[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+      for (uint32_t r = 0; r < kSpanRows; ++r) {
+        const uint32_t ty = o.y0 + r;
+        if (ty >= o.y1) break;
+        uint32_t lo;
+        const uint32_t len = row_span(e, ty, o.x0, o.x1, sp.tile_size, lo);
+        count += len;
+        w[r >> 1] |= ((lo - o.x0) | (len << 8)) << (16u * (r & 1u));
+      }
+      if (keep) {
+        b.rowspans[item] = make_uint4(w[0], w[1], w[2], w[3]);
+      } else {
+        uint32_t lo;
+        for (uint32_t ty = o.y0 + kSpanRows; ty < o.y1; ++ty)
+          count += row_span(e, ty, o.x0, o.x1, sp.tile_size, lo);
+      }
     }
   }
   b.aux[item] = make_float2(o.depth, o.radius);
@@ -429,13 +450,7 @@ __global__ void __launch_bounds__(256, 6) k_emit(DevBuffers b) {
   const uint32_t end = b.perm ? b.item_end[item] : b.cumsum[item];
   const uint32_t ikey = b.ikeys[item];
   const uint2 rc = b.rects[item];
-  float4 r0 = make_float4(0.f, 0.f, 0.f, 0.f);
-  float cc = 0.f, smax = 0.f;
-  if (sp.tile_cull) {
-    r0 = b.records[(size_t)item * 3 + 0];
-    cc = b.records[(size_t)item * 3 + 1].x;
-    smax = b.records[(size_t)item * 3 + 2].y;
-  }
+  const uint4 spans = sp.tile_cull ? b.rowspans[item] : make_uint4(0u, 0u, 0u, 0u);
   if (cnt == 0u) return;
   if (end > sp.icap || cnt > end) {
     atomicOr(&b.status->error, SKY_DEVERR_LISTS);
@@ -456,10 +471,37 @@ __global__ void __launch_bounds__(256, 6) k_emit(DevBuffers b) {
       }
     return;
   }
-  // culled: the tiles the preprocess counted, by the same test on the same
-  // record values
+  // culled: the tiles the preprocess counted -- its row spans where it kept
+  // them, else the same test on the same record values
+  if (!sp.tile_cull) {
+    atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
+    return;
+  }
+  if (y1 - y0 <= kSpanRows && x1 - x0 <= 255u) {
+    for (uint32_t r = 0; r < y1 - y0; ++r) {
+      const uint32_t wv = r < 2u ? spans.x : (r < 4u ? spans.y : (r < 6u ? spans.z : spans.w));
+      const uint32_t h = (wv >> (16u * (r & 1u))) & 0xFFFFu;
+      const uint32_t lo = x0 + (h & 0xFFu), len = h >> 8;
+      if (len > end - cur) {
+        atomicOr(&b.status->error, SKY_DEVERR_LISTS);
+        return;
+      }
+      const uint32_t ty = y0 + r;
+      for (uint32_t tx = lo; tx < lo + len; ++tx) {
+        const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
+        b.keys[cur] = (kt << 16) | dq;
+        b.rec_of[cur] = item;
+        ++cur;
+      }
+    }
+    if (cur != end) atomicOr(&b.status->error, SKY_DEVERR_LISTS);
+    return;
+  }
+  const float4 r0 = b.records[(size_t)item * 3 + 0];
+  const float cc = b.records[(size_t)item * 3 + 1].x;
+  const float smax = b.records[(size_t)item * 3 + 2].y;
   EllipseRows e;
-  if (!sp.tile_cull || !ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
+  if (!ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
     atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
     return;
   }

@@ -82,6 +82,8 @@ struct DevBuffers {
   float2* aux;        // depth, radius per item
   uint32_t* counts;   // tiles per item
   uint2* rects;       // packed tile rectangle per item
+  uint4* rowspans;    // culled lists: per item of at most kSpanRows rows, each row's
+                      // tile span (first tile - x0, length) as two bytes
   uint32_t* ikeys;    // per item (min(count, 0xFFFF) << 16) | depth16; sorted on depth16
                       // per group
   uint32_t* ikeys_sorted;  // the item keys in emission (perm) order
