@@ -461,65 +461,47 @@ __global__ void __launch_bounds__(256, 6) k_emit(DevBuffers b) {
   const uint32_t area = (x1 <= x0 || y1 <= y0) ? 0u : (x1 - x0) * (y1 - y0);
   uint32_t cur = end - cnt;
   const ViewInfo& vi = sp.views[v];
-  if (cnt == area) {
-    for (uint32_t ty = y0; ty < y1; ++ty)
-      for (uint32_t tx = x0; tx < x1; ++tx) {
-        const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
-        b.keys[cur] = (kt << 16) | dq;
-        b.rec_of[cur] = item;
-        ++cur;
-      }
-    return;
-  }
-  // culled: the tiles the preprocess counted -- its row spans where it kept
-  // them, else the same test on the same record values
-  if (!sp.tile_cull) {
-    atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
-    return;
-  }
-  if (y1 - y0 <= kSpanRows && x1 - x0 <= 255u) {
-    for (uint32_t r = 0; r < y1 - y0; ++r) {
-      const uint32_t wv = r < 2u ? spans.x : (r < 4u ? spans.y : (r < 6u ? spans.z : spans.w));
-      const uint32_t h = (wv >> (16u * (r & 1u))) & 0xFFFFu;
-      const uint32_t lo = x0 + (h & 0xFFu), len = h >> 8;
-      if (len > end - cur) {
-        atomicOr(&b.status->error, SKY_DEVERR_LISTS);
-        return;
-      }
-      const uint32_t ty = y0 + r;
-      for (uint32_t tx = lo; tx < lo + len; ++tx) {
-        const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
-        b.keys[cur] = (kt << 16) | dq;
-        b.rec_of[cur] = item;
-        ++cur;
-      }
-    }
-    if (cur != end) atomicOr(&b.status->error, SKY_DEVERR_LISTS);
-    return;
-  }
-  const float4 r0 = b.records[(size_t)item * 3 + 0];
-  const float cc = b.records[(size_t)item * 3 + 1].x;
-  const float smax = b.records[(size_t)item * 3 + 2].y;
-  EllipseRows e;
-  if (!ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e)) {
-    atomicOr(&b.status->error, SKY_DEVERR_LISTS);  // counted differently: corrupt lists
-    return;
-  }
-  for (uint32_t ty = y0; ty < y1; ++ty) {
-    uint32_t lo;
-    const uint32_t len = row_span(e, ty, x0, x1, sp.tile_size, lo);
-    if (len > end - cur) {
-      atomicOr(&b.status->error, SKY_DEVERR_LISTS);
-      return;
-    }
+  // the keys of tiles [lo, lo + len) of tile row ty; false: the row holds
+  // more tiles than the item's range has left (lists counted differently)
+  auto emit_row = [&](uint32_t ty, uint32_t lo, uint32_t len) {
+    if (len > end - cur) return false;
     for (uint32_t tx = lo; tx < lo + len; ++tx) {
       const uint32_t kt = vi.key_tile_base + ty * vi.tiles_x + tx;
       b.keys[cur] = (kt << 16) | dq;
       b.rec_of[cur] = item;
       ++cur;
     }
+    return true;
+  };
+  bool ok = true;
+  if (cnt == area) {
+    for (uint32_t ty = y0; ty < y1; ++ty) emit_row(ty, x0, x1 - x0);
+    return;
   }
-  if (cur != end) atomicOr(&b.status->error, SKY_DEVERR_LISTS);
+  // culled: the tiles the preprocess counted -- its row spans where it kept
+  // them, else the same test on the same record values
+  if (!sp.tile_cull) {
+    ok = false;
+  } else if (y1 - y0 <= kSpanRows && x1 - x0 <= 255u) {
+    for (uint32_t r = 0; ok && r < y1 - y0; ++r) {
+      const uint32_t wv = r < 2u ? spans.x : (r < 4u ? spans.y : (r < 6u ? spans.z : spans.w));
+      const uint32_t h = (wv >> (16u * (r & 1u))) & 0xFFFFu;
+      ok = emit_row(y0 + r, x0 + (h & 0xFFu), h >> 8);
+    }
+  } else {
+    const float4 r0 = b.records[(size_t)item * 3 + 0];
+    const float cc = b.records[(size_t)item * 3 + 1].x;
+    const float smax = b.records[(size_t)item * 3 + 2].y;
+    EllipseRows e;
+    ok = ellipse_rows(r0.x, r0.y, r0.z, r0.w, cc, smax, e);
+    for (uint32_t ty = y0; ok && ty < y1; ++ty) {
+      uint32_t lo;
+      const uint32_t len = row_span(e, ty, x0, x1, sp.tile_size, lo);
+      ok = emit_row(ty, lo, len);
+    }
+  }
+  // counted differently from the preprocess: corrupt lists
+  if (!ok || cur != end) atomicOr(&b.status->error, SKY_DEVERR_LISTS);
 }
 
 // ---------------------------------------------------------------------------
