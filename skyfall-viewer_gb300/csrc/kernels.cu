@@ -1309,12 +1309,13 @@ SKY_DEV void lane_moments(float val[9], float dx) {
 struct ColFactors {
   float a1, b1, c1, a2, b2;
 };
+// The row group's outputs u0, u1 f1, u1 f2 per case:
 SKY_DEV ColFactors col_factors(uint32_t lane) {
   switch ((lane >> 3) & 3u) {
-    case 0: return {1.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // c1 (x1), -
-    case 1: return {0.0f, 0.0f, 1.0f, 0.0f, 1.0f};  // g dx^2, g dx
-    case 2: return {0.0f, 1.0f, 0.0f, 1.0f, 0.0f};  // g dy dx, g dy
-    default: return {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+    case 0: return {1.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // c0, c1, (0)
+    case 1: return {0.0f, 0.0f, 1.0f, 0.0f, 1.0f};  // c2, g dx^2, g dx
+    case 2: return {0.0f, 1.0f, 0.0f, 1.0f, 0.0f};  // o, g dy dx, g dy
+    default: return {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};  // g dy^2, (0), (0)
   }
 }
 SKY_DEV int cols9_slot(uint32_t lane) {
